@@ -1,0 +1,108 @@
+"""ctypes binding of ``libgmes_gb300.so`` (include/gmes_gb300.h).
+
+The structures below mirror the header field for field.  Loading fails
+loudly when the library is missing: the package has no CPU fallback.
+"""
+
+import ctypes as C
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libgmes_gb300.so"
+
+ABI_VERSION = 1
+MAX_CLASSES = 256
+MAX_PML = 4
+MAX_POLES = 8
+
+FP64, FP32, DF64, FP64_STRICT = 0, 1, 2, 3
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "df64": DF64, "fp64_strict": FP64_STRICT}
+FLAG_DISPERSIVE = 1
+
+EXPORTS = [
+    "gmes_abi_version", "gmes_last_error", "gmes_elem_size", "gmes_field_shape",
+    "gmes_grid_sizes", "gmes_build_coefficients", "gmes_set_pml_profile",
+    "gmes_get_pml_profile", "gmes_reset",
+    "gmes_step", "gmes_read_field", "gmes_write_field",
+]
+
+
+class ClassDescC(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("pml", C.c_int32), ("npole", C.c_int32),
+                ("ncp", C.c_int32), ("param_off", C.c_int32), ("nparam", C.c_int32),
+                ("eps", C.c_double)]
+
+
+class PmlDescC(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("pad", C.c_int32), ("sigma_max", C.c_double * 3),
+                ("m", C.c_double), ("kappa_max", C.c_double), ("m_a", C.c_double),
+                ("a_max", C.c_double), ("d", C.c_double), ("center", C.c_double * 3),
+                ("half_size", C.c_double * 3)]
+
+
+class PointSourceC(C.Structure):
+    _fields_ = [("comp", C.c_int32), ("mode", C.c_int32), ("offset", C.c_int64)]
+
+
+class GridDescC(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_int32), ("precision", C.c_int32), ("n", C.c_int32 * 3),
+        ("active", C.c_int32), ("naux", C.c_int32 * 6), ("nclass", C.c_int32 * 6),
+        ("npml", C.c_int32), ("nsrc", C.c_int32), ("nparam", C.c_int32),
+        ("src_steps", C.c_int32), ("flags", C.c_int32), ("reserved", C.c_int32),
+        ("dr", C.c_double * 3), ("half", C.c_double * 3), ("dt", C.c_double),
+        ("field", C.c_void_p * 6), ("cls", C.c_void_p * 6), ("aux", C.c_void_p * 6),
+        ("coef", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p),
+    ]
+
+
+class GmesError(RuntimeError):
+    """Base of the errors raised for a failed engine call."""
+
+
+_STATUS_EXC = {1: ValueError, 2: IndexError, 3: RuntimeError, 4: RuntimeError}
+
+_lib = None
+
+
+def load():
+    """The loaded engine library (built on first use when nvcc is present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        from . import build as _build
+        _build.build()
+    lib = C.CDLL(str(LIB_PATH))
+    P = C.POINTER
+    lib.gmes_abi_version.restype = C.c_int
+    lib.gmes_last_error.restype = C.c_char_p
+    lib.gmes_elem_size.restype = C.c_int
+    lib.gmes_elem_size.argtypes = [C.c_int32]
+    lib.gmes_field_shape.argtypes = [P(GridDescC), C.c_int32, P(C.c_int64)]
+    lib.gmes_grid_sizes.argtypes = [P(GridDescC), P(C.c_int64)]
+    lib.gmes_build_coefficients.argtypes = [P(GridDescC), P(ClassDescC), P(C.c_double),
+                                            P(PmlDescC), C.c_void_p]
+    lib.gmes_set_pml_profile.argtypes = [P(GridDescC), C.c_int32, C.c_int32, C.c_int32,
+                                         P(C.c_double), C.c_void_p]
+    lib.gmes_get_pml_profile.argtypes = [P(GridDescC), C.c_int32, C.c_int32, C.c_int32,
+                                         P(C.c_double), C.c_void_p]
+    lib.gmes_reset.argtypes = [P(GridDescC), C.c_void_p]
+    lib.gmes_step.argtypes = [P(GridDescC), C.c_int32, C.c_void_p]
+    lib.gmes_read_field.argtypes = [P(GridDescC), C.c_int32, P(C.c_double), C.c_void_p]
+    lib.gmes_write_field.argtypes = [P(GridDescC), C.c_int32, P(C.c_double), C.c_void_p]
+    for name in EXPORTS:
+        if name not in ("gmes_abi_version", "gmes_last_error", "gmes_elem_size"):
+            getattr(lib, name).restype = C.c_int
+    if lib.gmes_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{LIB_PATH}: ABI {lib.gmes_abi_version()}, expected {ABI_VERSION}")
+    _lib = lib
+    return lib
+
+
+def check(status):
+    """Raise the Python exception matching a non-zero gmes_status."""
+    if status == 0:
+        return
+    msg = load().gmes_last_error().decode(errors="replace")
+    raise _STATUS_EXC.get(status, RuntimeError)(msg)

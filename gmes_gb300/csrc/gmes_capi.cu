@@ -1,0 +1,407 @@
+// extern "C" entry points of libgmes_gb300.so: argument validation, the
+// coefficient-block layout, host<->device staging and error reporting.
+// Status codes follow the reference binding's exception classes
+// (src/pw_material.i:23-33): ValueError, IndexError, RuntimeError.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gmes_internal.cuh"
+
+namespace gmes {
+namespace {
+
+thread_local std::string g_last_error;
+
+gmes_status fail(gmes_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return st;
+}
+
+gmes_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(GMES_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+int elem_size(int32_t precision) {
+  switch (precision) {
+    case GMES_FP64:
+    case GMES_FP64_STRICT:
+    case GMES_DF64:
+      return 8;
+    case GMES_FP32:
+      return 4;
+    default:
+      return 0;
+  }
+}
+
+// Validate everything that can be checked without touching device memory.
+gmes_status check_desc(const gmes_grid_desc* g, bool need_buffers) {
+  if (g == nullptr) return fail(GMES_ERR_VALUE, "grid descriptor is NULL");
+  if (g->abi_version != GMES_ABI_VERSION)
+    return fail(GMES_ERR_VALUE, "ABI version mismatch: descriptor %d, library %d",
+                g->abi_version, GMES_ABI_VERSION);
+  if (elem_size(g->precision) == 0)
+    return fail(GMES_ERR_VALUE, "unknown precision %d", g->precision);
+  for (int a = 0; a < 3; ++a) {
+    if (g->n[a] < 1) return fail(GMES_ERR_VALUE, "grid size n[%d] = %d must be >= 1", a, g->n[a]);
+    if (!(g->dr[a] > 0) || !std::isfinite(g->dr[a]))
+      return fail(GMES_ERR_VALUE, "cell size dr[%d] must be positive and finite", a);
+  }
+  if (!(g->dt > 0) || !std::isfinite(g->dt)) return fail(GMES_ERR_VALUE, "dt must be positive");
+  if ((g->active & ~63) != 0 || (g->active & 7) == 0 || (g->active & 56) == 0)
+    return fail(GMES_ERR_VALUE, "active mask 0x%x must name at least one E and one H component",
+                g->active);
+  if (g->npml < 0 || g->npml > GMES_MAX_PML)
+    return fail(GMES_ERR_VALUE, "npml = %d outside [0, %d]", g->npml, GMES_MAX_PML);
+  if (g->nsrc < 0 || g->nparam < 0 || g->src_steps < 0)
+    return fail(GMES_ERR_VALUE, "negative nsrc / nparam / src_steps");
+  for (int c = 0; c < 6; ++c) {
+    const bool act = (g->active >> c) & 1;
+    if (g->nclass[c] < 0 || g->nclass[c] > GMES_MAX_CLASSES)
+      return fail(GMES_ERR_VALUE, "nclass[%d] = %d outside [0, %d]", c, g->nclass[c],
+                  GMES_MAX_CLASSES);
+    if (act && g->nclass[c] < 1)
+      return fail(GMES_ERR_VALUE, "active component %d has no classes", c);
+    if (g->naux[c] < 0 || g->naux[c] > 1 + 4 * GMES_MAX_POLES)
+      return fail(GMES_ERR_VALUE, "naux[%d] = %d out of range", c, g->naux[c]);
+    if (need_buffers) {
+      if (g->field[c] == nullptr) return fail(GMES_ERR_VALUE, "field[%d] is NULL", c);
+      if (act && g->cls[c] == nullptr) return fail(GMES_ERR_VALUE, "cls[%d] is NULL", c);
+      if (act && g->naux[c] > 0 && g->aux[c] == nullptr)
+        return fail(GMES_ERR_VALUE, "aux[%d] is NULL but naux[%d] = %d", c, c, g->naux[c]);
+    }
+  }
+  if (need_buffers && g->coef == nullptr) return fail(GMES_ERR_VALUE, "coef is NULL");
+  if (need_buffers && g->nsrc > 0 && (g->src == nullptr || g->src_val == nullptr))
+    return fail(GMES_ERR_VALUE, "nsrc > 0 but src or src_val is NULL");
+  return GMES_OK;
+}
+
+}  // namespace
+
+GridDev make_grid_dev(const gmes_grid_desc& g) {
+  GridDev d;
+  std::memset(&d, 0, sizeof(d));
+  for (int a = 0; a < 3; ++a) {
+    d.n[a] = g.n[a];
+    d.dr[a] = g.dr[a];
+  }
+  d.dt = g.dt;
+  d.active = g.active;
+  d.nsrc = g.nsrc;
+  const CoefLayout L = coef_layout(g);
+  char* base = static_cast<char*>(g.coef);
+  for (int c = 0; c < 6; ++c) {
+    int64_t sh[3];
+    comp_shape(g.n, g.active, c, sh);
+    for (int a = 0; a < 3; ++a) d.sh[c][a] = sh[a];
+    d.st[c][0] = sh[1] * sh[2];
+    d.st[c][1] = sh[2];
+    d.npts[c] = sh[0] * sh[1] * sh[2];
+    d.f[c] = g.field[c];
+    d.cls[c] = g.cls[c];
+    d.aux[c] = g.aux[c];
+    d.tab[c] = reinterpret_cast<const ClassCoef*>(base + L.class_tab[c]);
+    d.pool[c] = reinterpret_cast<const Coef*>(base + L.pool[c]);
+    for (int p = 0; p < GMES_MAX_PML; ++p)
+      for (int a = 0; a < 3; ++a)
+        d.prof[p][c][a] = reinterpret_cast<const Coef*>(base + L.prof[p][c][a]);
+  }
+  d.src = g.src;
+  d.src_val = g.src_val;
+  return d;
+}
+
+}  // namespace gmes
+
+using namespace gmes;
+
+extern "C" {
+
+int gmes_abi_version(void) { return GMES_ABI_VERSION; }
+
+const char* gmes_last_error(void) { return g_last_error.c_str(); }
+
+int gmes_elem_size(int32_t precision) { return elem_size(precision); }
+
+gmes_status gmes_field_shape(const gmes_grid_desc* g, int32_t comp, int64_t shape[3]) {
+  if (g == nullptr || shape == nullptr) return fail(GMES_ERR_VALUE, "NULL argument");
+  if (comp < 0 || comp > 5) return fail(GMES_ERR_INDEX, "component %d outside [0, 5]", comp);
+  comp_shape(g->n, g->active, comp, shape);
+  return GMES_OK;
+}
+
+gmes_status gmes_grid_sizes(const gmes_grid_desc* g, int64_t sizes[21]) {
+  gmes_status st = check_desc(g, false);
+  if (st != GMES_OK) return st;
+  if (sizes == nullptr) return fail(GMES_ERR_VALUE, "sizes is NULL");
+  const int es = elem_size(g->precision);
+  for (int c = 0; c < 6; ++c) {
+    int64_t sh[3];
+    comp_shape(g->n, g->active, c, sh);
+    const int64_t np = sh[0] * sh[1] * sh[2];
+    const bool act = (g->active >> c) & 1;
+    sizes[c] = np * es;
+    sizes[6 + c] = act ? np : 0;
+    sizes[12 + c] = act ? np * es * g->naux[c] : 0;
+  }
+  sizes[18] = coef_layout(*g).total;
+  sizes[19] = (int64_t)g->nsrc * (int64_t)sizeof(gmes_point_source);
+  sizes[20] = 2 * (int64_t)g->nsrc * (int64_t)sizeof(double);
+  return GMES_OK;
+}
+
+gmes_status gmes_build_coefficients(const gmes_grid_desc* g, const gmes_class_desc* classes,
+                                    const double* params, const gmes_pml_desc* pmls,
+                                    void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  int ncls = 0;
+  for (int c = 0; c < 6; ++c) ncls += g->nclass[c];
+  if (ncls > 0 && classes == nullptr) return fail(GMES_ERR_VALUE, "classes is NULL");
+  if (g->nparam > 0 && params == nullptr) return fail(GMES_ERR_VALUE, "params is NULL");
+  if (g->npml > 0 && pmls == nullptr) return fail(GMES_ERR_VALUE, "pmls is NULL");
+  // validate the class table against the pool and the PML list
+  int k = 0;
+  bool disp = false;
+  for (int c = 0; c < 6; ++c) {
+    for (int i = 0; i < g->nclass[c]; ++i, ++k) {
+      const gmes_class_desc& cd = classes[k];
+      if (cd.kind < GMES_KIND_DUMMY || cd.kind > GMES_KIND_CONST)
+        return fail(GMES_ERR_VALUE, "component %d class %d: unknown kind %d", c, i, cd.kind);
+      if ((cd.kind == GMES_KIND_CPML || cd.kind == GMES_KIND_UPML) &&
+          (cd.pml < 0 || cd.pml >= g->npml))
+        return fail(GMES_ERR_INDEX, "component %d class %d: pml index %d out of range", c, i,
+                    cd.pml);
+      if ((cd.kind == GMES_KIND_CPML || cd.kind == GMES_KIND_UPML) &&
+          pmls[cd.pml].kind != cd.kind)
+        return fail(GMES_ERR_VALUE, "component %d class %d: PML kind mismatch", c, i);
+      if (cd.param_off < 0 || cd.nparam < 0 || cd.param_off + cd.nparam > g->nparam)
+        return fail(GMES_ERR_INDEX, "component %d class %d: parameters outside the pool", c, i);
+      if (cd.npole < 0 || cd.npole > GMES_MAX_POLES || cd.ncp < 0 || cd.ncp > GMES_MAX_POLES)
+        return fail(GMES_ERR_VALUE, "component %d class %d: at most %d poles", c, i,
+                    GMES_MAX_POLES);
+      if (!(cd.eps > 0) && cd.kind != GMES_KIND_DUMMY && cd.kind != GMES_KIND_CONST)
+        return fail(GMES_ERR_VALUE, "component %d class %d: eps/mu must be positive", c, i);
+      int need = 0, naux = 0;
+      switch (cd.kind) {
+        case GMES_KIND_CONST: need = 1; break;
+        case GMES_KIND_DRUDE: need = 2 + 2 * cd.npole; naux = 2 * cd.npole; break;
+        case GMES_KIND_LORENTZ: need = 2 + 3 * cd.npole; naux = 2 * cd.npole; break;
+        case GMES_KIND_DCP: need = 2 + 2 * cd.npole + 5 * cd.ncp;
+          naux = 1 + 2 * cd.npole + 2 * cd.ncp; break;
+        case GMES_KIND_CPML: naux = 2; break;
+        case GMES_KIND_UPML: naux = 1; break;
+        default: break;
+      }
+      const bool dispk = cd.kind == GMES_KIND_DRUDE || cd.kind == GMES_KIND_LORENTZ ||
+                         cd.kind == GMES_KIND_DCP;
+      if (dispk && c >= 3)
+        return fail(GMES_ERR_VALUE, "component %d class %d: dispersive kinds are E-only", c, i);
+      disp = disp || dispk;
+      if (cd.nparam < need)
+        return fail(GMES_ERR_VALUE, "component %d class %d: %d parameters, kind needs %d", c,
+                    i, cd.nparam, need);
+      if (naux > g->naux[c])
+        return fail(GMES_ERR_VALUE, "component %d class %d needs %d state slots, naux = %d", c,
+                    i, naux, g->naux[c]);
+    }
+  }
+  if (disp && !(g->flags & GMES_FLAG_DISPERSIVE))
+    return fail(GMES_ERR_VALUE, "dispersive classes present but GMES_FLAG_DISPERSIVE unset");
+  const CoefLayout L = coef_layout(*g);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(g->coef);
+  cudaError_t e = cudaSuccess;
+  if (ncls > 0)
+    e = cudaMemcpyAsync(base + L.raw_classes, classes, ncls * sizeof(gmes_class_desc),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && g->nparam > 0)
+    e = cudaMemcpyAsync(base + L.raw_params, params, g->nparam * sizeof(double),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && g->npml > 0)
+    e = cudaMemcpyAsync(base + L.raw_pmls, pmls, g->npml * sizeof(gmes_pml_desc),
+                        cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "staging coefficient inputs");
+  for (int c = 0; c < 6 && e == cudaSuccess; ++c)
+    e = cudaMemsetAsync(base + L.class_tab[c], 0, GMES_MAX_CLASSES * sizeof(ClassCoef), s);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing class tables");
+  const GridDev d = make_grid_dev(*g);
+  e = launch_build_coefficients(*g, d, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "building coefficients");
+  return GMES_OK;
+}
+
+gmes_status gmes_set_pml_profile(const gmes_grid_desc* g, int32_t pml, int32_t comp,
+                                 int32_t axis, const double* values, void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  if (pml < 0 || pml >= g->npml) return fail(GMES_ERR_INDEX, "pml %d out of range", pml);
+  if (comp < 0 || comp > 5 || axis < 0 || axis > 2)
+    return fail(GMES_ERR_INDEX, "component %d / axis %d out of range", comp, axis);
+  if (!((g->active >> comp) & 1)) return fail(GMES_ERR_VALUE, "component %d inactive", comp);
+  if (values == nullptr) return fail(GMES_ERR_VALUE, "values is NULL");
+  const CoefLayout L = coef_layout(*g);
+  int64_t sh[3];
+  comp_shape(g->n, g->active, comp, sh);
+  // The kind of this PML is read back from the staged inputs.
+  gmes_pml_desc pd;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(g->coef);
+  cudaError_t e = cudaMemcpyAsync(&pd, base + L.raw_pmls + pml * sizeof(gmes_pml_desc),
+                                  sizeof(pd), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "reading PML descriptor");
+  std::vector<Coef> rows(sh[axis] * kProfStride);
+  const double dr = g->dr[axis], dt = g->dt;
+  for (int64_t n = 0; n < sh[axis]; ++n) {
+    const double* v = values + 3 * n;
+    Coef* out = rows.data() + n * kProfStride;
+    if (pd.kind == GMES_KIND_CPML) {
+      const double b = v[0], c = v[1], kappa = v[2];
+      out[0] = make_coef(b);
+      out[1] = make_coef(c);
+      out[2] = make_coef(kappa);
+      out[3] = make_coef(c / dr);
+      out[4] = make_coef(1.0 / (kappa * dr));
+    } else {
+      const double sigma = v[0], kappa = v[1];
+      const double num = 2 * kappa - sigma * dt, den = 2 * kappa + sigma * dt;
+      out[0] = make_coef(num / den);
+      out[1] = make_coef(2 * dt / den);
+      out[2] = make_coef(1 / den);
+      out[3] = make_coef(den);
+      out[4] = make_coef(num);
+    }
+  }
+  e = cudaMemcpyAsync(base + L.prof[pml][comp][axis], rows.data(), rows.size() * sizeof(Coef),
+                      cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "uploading PML profile");
+  return GMES_OK;
+}
+
+gmes_status gmes_get_pml_profile(const gmes_grid_desc* g, int32_t pml, int32_t comp,
+                                 int32_t axis, double* out, void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  if (pml < 0 || pml >= g->npml) return fail(GMES_ERR_INDEX, "pml %d out of range", pml);
+  if (comp < 0 || comp > 5 || axis < 0 || axis > 2)
+    return fail(GMES_ERR_INDEX, "component %d / axis %d out of range", comp, axis);
+  if (!((g->active >> comp) & 1)) return fail(GMES_ERR_VALUE, "component %d inactive", comp);
+  if (out == nullptr) return fail(GMES_ERR_VALUE, "out is NULL");
+  const CoefLayout L = coef_layout(*g);
+  int64_t sh[3];
+  comp_shape(g->n, g->active, comp, sh);
+  std::vector<Coef> rows(sh[axis] * kProfStride);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(rows.data(), static_cast<char*>(g->coef) + L.prof[pml][comp][axis],
+                                  rows.size() * sizeof(Coef), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "reading PML profile");
+  for (size_t i = 0; i < rows.size(); ++i) out[i] = rows[i].d;
+  return GMES_OK;
+}
+
+gmes_status gmes_reset(const gmes_grid_desc* g, void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  int64_t sizes[21];
+  gmes_grid_sizes(g, sizes);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  for (int c = 0; c < 6; ++c) {
+    cudaError_t e = cudaMemsetAsync(g->field[c], 0, sizes[c], s);
+    if (e == cudaSuccess && sizes[12 + c] > 0) e = cudaMemsetAsync(g->aux[c], 0, sizes[12 + c], s);
+    if (e != cudaSuccess) return cuda_fail(e, "zeroing buffers");
+  }
+  return GMES_OK;
+}
+
+gmes_status gmes_step(const gmes_grid_desc* g, int32_t nsteps, void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  if (nsteps < 0) return fail(GMES_ERR_VALUE, "nsteps = %d must be >= 0", nsteps);
+  if (g->nsrc > 0 && nsteps > g->src_steps)
+    return fail(GMES_ERR_VALUE, "nsteps = %d exceeds the source-value capacity %d", nsteps,
+                g->src_steps);
+  if (nsteps == 0) return GMES_OK;
+  const GridDev d = make_grid_dev(*g);
+  cudaError_t e = launch_step(*g, d, nsteps, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching step kernels");
+  return GMES_OK;
+}
+
+gmes_status gmes_read_field(const gmes_grid_desc* g, int32_t comp, double* host_out,
+                            void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  if (comp < 0 || comp > 5) return fail(GMES_ERR_INDEX, "component %d outside [0, 5]", comp);
+  if (host_out == nullptr) return fail(GMES_ERR_VALUE, "host_out is NULL");
+  int64_t sh[3];
+  comp_shape(g->n, g->active, comp, sh);
+  const int64_t np = sh[0] * sh[1] * sh[2];
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (g->precision == GMES_FP64 || g->precision == GMES_FP64_STRICT) {
+    e = cudaMemcpyAsync(host_out, g->field[comp], np * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  } else if (g->precision == GMES_FP32) {
+    std::vector<float> tmp(np);
+    e = cudaMemcpyAsync(tmp.data(), g->field[comp], np * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    for (int64_t i = 0; e == cudaSuccess && i < np; ++i) host_out[i] = tmp[i];
+  } else {
+    std::vector<float> tmp(2 * np);
+    e = cudaMemcpyAsync(tmp.data(), g->field[comp], np * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    for (int64_t i = 0; e == cudaSuccess && i < np; ++i)
+      host_out[i] = (double)tmp[2 * i] + (double)tmp[2 * i + 1];
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "reading field");
+  return GMES_OK;
+}
+
+gmes_status gmes_write_field(const gmes_grid_desc* g, int32_t comp, const double* host_in,
+                             void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  if (comp < 0 || comp > 5) return fail(GMES_ERR_INDEX, "component %d outside [0, 5]", comp);
+  if (host_in == nullptr) return fail(GMES_ERR_VALUE, "host_in is NULL");
+  int64_t sh[3];
+  comp_shape(g->n, g->active, comp, sh);
+  const int64_t np = sh[0] * sh[1] * sh[2];
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (g->precision == GMES_FP64 || g->precision == GMES_FP64_STRICT) {
+    e = cudaMemcpyAsync(g->field[comp], host_in, np * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  } else if (g->precision == GMES_FP32) {
+    std::vector<float> tmp(np);
+    for (int64_t i = 0; i < np; ++i) tmp[i] = (float)host_in[i];
+    e = cudaMemcpyAsync(g->field[comp], tmp.data(), np * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  } else {
+    std::vector<float> tmp(2 * np);
+    for (int64_t i = 0; i < np; ++i) {
+      const float h = (float)host_in[i];
+      tmp[2 * i] = h;
+      tmp[2 * i + 1] = (float)(host_in[i] - (double)h);
+    }
+    e = cudaMemcpyAsync(g->field[comp], tmp.data(), np * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "writing field");
+  return GMES_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,240 @@
+// Internal definitions shared by the engine's translation units:
+// coefficient-block layout (host and device agree through the same
+// functions), the kernel-side grid view, and the three arithmetic policies
+// (FP64, FP32, float-float).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gmes_gb300.h"
+
+namespace gmes {
+
+// ---------------------------------------------------------------------------
+// Coefficients.  Every coefficient is computed once in FP64 on the GPU and
+// stored in three forms so no kernel converts on the hot path:
+//   d  -- FP64 (GMES_FP64, GMES_FP64_STRICT)
+//   hi -- FP32 round-to-nearest of d (GMES_FP32; high word of GMES_DF64)
+//   lo -- FP32 of (d - hi)  (low word of GMES_DF64)
+// ---------------------------------------------------------------------------
+struct Coef {
+  double d;
+  float hi, lo;
+};
+
+__host__ __device__ inline Coef make_coef(double v) {
+  Coef c;
+  c.d = v;
+  c.hi = static_cast<float>(v);
+  c.lo = static_cast<float>(v - static_cast<double>(c.hi));
+  return c;
+}
+
+// Per (component, class) entry of the class table.
+struct ClassCoef {
+  int32_t kind, pml, npole, ncp;
+  int32_t pad[4];
+  Coef eps;   // eps_inf (E) / mu_inf (H)
+  Coef cdt;   // dt / eps
+  Coef c1;    // dt / eps / d1   (d1, d2: cell sizes of the two curl axes)
+  Coef c2;    // dt / eps / d2
+  Coef reps;  // 1 / eps
+  Coef value; // CONST
+};
+
+// Dispersive coefficients of one class: a[p][3] (Drude/Lorentz poles or DCP
+// Drude terms), b[q][5] (DCP critical points), c[4].
+constexpr int kPoolA = 0;
+constexpr int kPoolB = 3 * GMES_MAX_POLES;
+constexpr int kPoolC = kPoolB + 5 * GMES_MAX_POLES;
+constexpr int kPoolStride = kPoolC + 4;
+
+// PML profile entry at one index along one axis (5 coefficients):
+//   CPML: b, c, kappa, c / d, 1 / (kappa d)
+//   UPML: c1 (= c3), c2, c4, c5, c6     (src/material.pyx:558-591)
+constexpr int kProfStride = 5;
+
+// Yee staggering, rows Ex..Hz (gmes/geometry.py:360-732).
+__host__ __device__ inline double yee_offset(int c, int axis) {
+  if (c < 3) return axis == c ? 0.5 : 0.0;
+  return axis == c - 3 ? 0.0 : -0.5;
+}
+
+__host__ __device__ inline void comp_shape(const int32_t n[3], int32_t active, int c,
+                                           int64_t sh[3]) {
+  if (!(active & (1 << c))) {
+    sh[0] = sh[1] = sh[2] = 1;
+    return;
+  }
+  const int own = c % 3;
+  for (int a = 0; a < 3; ++a) sh[a] = a == own ? n[a] : n[a] + 1;
+}
+
+__host__ __device__ inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
+
+// Coefficient block layout (offsets in bytes from g.coef).
+struct CoefLayout {
+  int64_t raw_classes;  // gmes_class_desc[sum nclass] (host input staging)
+  int64_t raw_params;   // double[nparam]
+  int64_t raw_pmls;     // gmes_pml_desc[npml]
+  int64_t class_tab[6]; // ClassCoef[nclass[c]]
+  int64_t pool[6];      // Coef[nclass[c] * kPoolStride]
+  int64_t prof[GMES_MAX_PML][6][3];  // Coef[shape[c][axis] * kProfStride]
+  int64_t total;
+};
+
+__host__ __device__ inline CoefLayout coef_layout(const gmes_grid_desc& g) {
+  CoefLayout L;
+  int64_t off = 0;
+  int64_t ncls = 0;
+  for (int c = 0; c < 6; ++c) ncls += g.nclass[c];
+  L.raw_classes = off;
+  off = align256(off + ncls * (int64_t)sizeof(gmes_class_desc));
+  L.raw_params = off;
+  off = align256(off + (int64_t)g.nparam * 8);
+  L.raw_pmls = off;
+  off = align256(off + (int64_t)g.npml * (int64_t)sizeof(gmes_pml_desc));
+  // Every component gets a full 256-entry class table: a class id without a
+  // class (any u8 value) reads a zeroed entry, i.e. kind DUMMY -- no update.
+  for (int c = 0; c < 6; ++c) {
+    L.class_tab[c] = off;
+    off = align256(off + (int64_t)GMES_MAX_CLASSES * (int64_t)sizeof(ClassCoef));
+  }
+  for (int c = 0; c < 6; ++c) {
+    L.pool[c] = off;
+    off = align256(off + (int64_t)g.nclass[c] * kPoolStride * (int64_t)sizeof(Coef));
+  }
+  for (int p = 0; p < GMES_MAX_PML; ++p)
+    for (int c = 0; c < 6; ++c)
+      for (int a = 0; a < 3; ++a) {
+        L.prof[p][c][a] = off;
+        if (p < g.npml) {
+          int64_t sh[3];
+          comp_shape(g.n, g.active, c, sh);
+          off = align256(off + sh[a] * kProfStride * (int64_t)sizeof(Coef));
+        }
+      }
+  L.total = align256(off);
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel-side view of a grid (passed by value as a kernel parameter).
+// ---------------------------------------------------------------------------
+struct GridDev {
+  int32_t n[3];
+  int32_t active;
+  int32_t nsrc;
+  int32_t pad;
+  int64_t sh[6][3];       // component shapes
+  int64_t st[6][2];       // strides of axes 0 and 1 (axis 2 stride is 1)
+  int64_t npts[6];        // points per component
+  void* f[6];
+  const uint8_t* cls[6];
+  void* aux[6];
+  const ClassCoef* tab[6];
+  const Coef* pool[6];
+  const Coef* prof[GMES_MAX_PML][6][3];
+  const gmes_point_source* src;
+  const double* src_val;
+  double dr[3];
+  double dt;
+};
+
+// ---------------------------------------------------------------------------
+// Arithmetic policies.
+// ---------------------------------------------------------------------------
+
+// Float-float number: value = hi + lo with |lo| <= ulp(hi)/2.  Operations are
+// the classical error-free transformations (Knuth two-sum, Dekker/FMA
+// two-product) written with round-to-nearest intrinsics so the compiler can
+// neither contract nor reassociate them.
+struct df {
+  float hi, lo;
+};
+
+__device__ __forceinline__ df df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+
+__device__ __forceinline__ df df_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ df operator+(df a, df b) {
+  df s = df_two_sum(a.hi, b.hi);
+  const df t = df_two_sum(a.lo, b.lo);
+  s.lo = __fadd_rn(s.lo, t.hi);
+  s = df_fast_two_sum(s.hi, s.lo);
+  s.lo = __fadd_rn(s.lo, t.lo);
+  return df_fast_two_sum(s.hi, s.lo);
+}
+
+__device__ __forceinline__ df operator-(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
+
+__device__ __forceinline__ df operator*(df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+
+struct PolF64 {
+  using T = double;
+  using R = double;
+  static __device__ __forceinline__ R ld(const T* p) { return __ldg(p); }
+  static __device__ __forceinline__ R ldw(const T* p) { return *p; }
+  static __device__ __forceinline__ void st(T* p, R v) { *p = v; }
+  static __device__ __forceinline__ R cf(const Coef& c) { return c.d; }
+  static __device__ __forceinline__ R zero() { return 0.0; }
+  static __device__ __forceinline__ R from_double(double v) { return v; }
+};
+
+struct PolF32 {
+  using T = float;
+  using R = float;
+  static __device__ __forceinline__ R ld(const T* p) { return __ldg(p); }
+  static __device__ __forceinline__ R ldw(const T* p) { return *p; }
+  static __device__ __forceinline__ void st(T* p, R v) { *p = v; }
+  static __device__ __forceinline__ R cf(const Coef& c) { return c.hi; }
+  static __device__ __forceinline__ R zero() { return 0.f; }
+  static __device__ __forceinline__ R from_double(double v) { return static_cast<float>(v); }
+};
+
+struct PolDF {
+  using T = float2;
+  using R = df;
+  static __device__ __forceinline__ R ld(const T* p) {
+    const float2 v = __ldg(p);
+    return {v.x, v.y};
+  }
+  static __device__ __forceinline__ R ldw(const T* p) {
+    const float2 v = *p;
+    return {v.x, v.y};
+  }
+  static __device__ __forceinline__ void st(T* p, R v) { *p = make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ R cf(const Coef& c) { return {c.hi, c.lo}; }
+  static __device__ __forceinline__ R zero() { return {0.f, 0.f}; }
+  static __device__ __forceinline__ R from_double(double v) {
+    const float h = static_cast<float>(v);
+    return {h, static_cast<float>(v - static_cast<double>(h))};
+  }
+};
+
+// Host-side helpers implemented in gmes_capi.cu.
+GridDev make_grid_dev(const gmes_grid_desc& g);
+
+// Launchers implemented per precision in gmes_step.cu.
+cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps,
+                        cudaStream_t s);
+cudaError_t launch_build_coefficients(const gmes_grid_desc& g, const GridDev& d,
+                                      cudaStream_t s);
+
+}  // namespace gmes

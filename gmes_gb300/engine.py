@@ -1,0 +1,244 @@
+"""One grid on the GPU: device buffers (torch tensors) + the C ABI.
+
+PyTorch only supplies device memory and the stream; all computation runs in
+the engine's own kernels (libgmes_gb300.so).  The buffers are sized by
+``gmes_grid_sizes`` and described to the library by a ``GridDescC``.
+"""
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .scene import class_arrays, source_offsets, source_values
+
+_TORCH = None
+
+
+def _torch():
+    global _TORCH
+    if _TORCH is None:
+        import torch
+        _TORCH = torch
+    return _TORCH
+
+
+def require_cuda():
+    torch = _torch()
+    if not torch.cuda.is_available():
+        raise RuntimeError("gmes_gb300 needs a CUDA GPU: no CUDA device is visible")
+
+
+class GridEngine:
+    """Device state of one FDTD grid.
+
+    ``precision``: "fp64" (default), "fp64_strict", "fp32" or "df64".
+    ``src_chunk``: steps of source values staged per ``gmes_step`` call.
+    """
+
+    def __init__(self, scene, precision="fp64", device=None, src_chunk=256):
+        require_cuda()
+        torch = _torch()
+        self.lib = N.load()
+        self.scene = scene
+        self.precision = precision
+        self.prec = N.PRECISIONS[precision]
+        self.device = torch.device(device if device is not None else "cuda")
+        self.src_chunk = int(src_chunk)
+        d = N.GridDescC()
+        d.abi_version = N.ABI_VERSION
+        d.precision = self.prec
+        for a in range(3):
+            d.n[a] = scene.n[a]
+            d.dr[a] = scene.dr[a]
+            d.half[a] = scene.half[a]
+        d.dt = scene.dt
+        d.active = scene.active_mask
+        for c in range(6):
+            d.naux[c] = scene.naux(c)
+            d.nclass[c] = len(scene.classes[c])
+        rows, pool, pmls = class_arrays(scene)
+        d.npml = len(pmls)
+        d.nsrc = len(scene.sources)
+        d.nparam = len(pool)
+        d.src_steps = self.src_chunk
+        d.flags = N.FLAG_DISPERSIVE if scene.dispersive else 0
+        sizes = (C.c_int64 * 21)()
+        N.check(self.lib.gmes_grid_sizes(C.byref(d), sizes))
+        self.sizes = list(sizes)
+        dev = self.device
+        self.fields = []
+        self.aux = []
+        self.cls = []
+        for c in range(6):
+            shape = scene.shape(c)
+            if self.prec in (N.FP64, N.FP64_STRICT):
+                t = torch.zeros(shape, dtype=torch.float64, device=dev)
+            elif self.prec == N.FP32:
+                t = torch.zeros(shape, dtype=torch.float32, device=dev)
+            else:
+                t = torch.zeros(shape + (2,), dtype=torch.float32, device=dev)
+            self.fields.append(t)
+            d.field[c] = t.data_ptr()
+            na = d.naux[c] if (scene.active_mask >> c) & 1 else 0
+            if na:
+                a = torch.zeros(self.sizes[12 + c], dtype=torch.uint8, device=dev)
+                d.aux[c] = a.data_ptr()
+            else:
+                a = None
+            self.aux.append(a)
+            if scene.cls[c] is not None:
+                m = torch.from_numpy(scene.cls[c]).to(dev)
+                d.cls[c] = m.data_ptr()
+            else:
+                m = None
+            self.cls.append(m)
+        self.coef = torch.zeros(max(self.sizes[18], 256), dtype=torch.uint8, device=dev)
+        d.coef = self.coef.data_ptr()
+        srcs = source_offsets(scene)
+        if srcs:
+            arr = (N.PointSourceC * len(srcs))(*[N.PointSourceC(c, m, o) for c, m, o in srcs])
+            host = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8)
+            self.src = host.to(dev)
+            self.src_val = torch.zeros((self.src_chunk, 2, len(srcs)), dtype=torch.float64,
+                                       device=dev)
+            self.src_host = torch.zeros(self.src_val.shape, dtype=torch.float64).pin_memory()
+            d.src = self.src.data_ptr()
+            d.src_val = self.src_val.data_ptr()
+        else:
+            self.src = self.src_val = self.src_host = None
+        self.desc = d
+        self._staged = None
+        self._rows, self._pool, self._pmls = rows, pool, pmls
+        self.build_coefficients()
+
+    # -- setup -------------------------------------------------------------
+    @property
+    def stream(self):
+        return _torch().cuda.current_stream(self.device).cuda_stream
+
+    def build_coefficients(self):
+        rows, pool, pmls = self._rows, self._pool, self._pmls
+        crow = (N.ClassDescC * max(1, len(rows)))()
+        for i, r in enumerate(rows):
+            crow[i] = N.ClassDescC(r["kind"], r["pml"], r["npole"], r["ncp"], r["param_off"],
+                                   r["nparam"], r["eps"])
+        cpool = (C.c_double * max(1, len(pool)))(*pool)
+        cpml = (N.PmlDescC * max(1, len(pmls)))()
+        for i, p in enumerate(pmls):
+            q = cpml[i]
+            q.kind = p["kind"]
+            for a in range(3):
+                q.sigma_max[a] = p["sigma_max"][a]
+                q.center[a] = p["center"][a]
+                q.half_size[a] = p["half_size"][a]
+            q.m, q.kappa_max, q.m_a, q.a_max, q.d = (p["m"], p["kappa_max"], p["m_a"],
+                                                      p["a_max"], p["d"])
+        N.check(self.lib.gmes_build_coefficients(C.byref(self.desc), crow, cpool, cpml,
+                                                 C.c_void_p(self.stream)))
+
+    def set_pml_profile(self, pml, comp, axis, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        N.check(self.lib.gmes_set_pml_profile(
+            C.byref(self.desc), pml, comp, axis,
+            v.ctypes.data_as(C.POINTER(C.c_double)), C.c_void_p(self.stream)))
+
+    def get_pml_profile(self, pml, comp, axis):
+        """FP64 profile rows (n, 5) of (pml, comp, axis) as computed on the GPU."""
+        n = self.scene.shape(comp)[axis]
+        out = np.zeros((n, 5), np.float64)
+        N.check(self.lib.gmes_get_pml_profile(
+            C.byref(self.desc), pml, comp, axis, out.ctypes.data_as(C.POINTER(C.c_double)),
+            C.c_void_p(self.stream)))
+        return out
+
+    def reset(self):
+        N.check(self.lib.gmes_reset(C.byref(self.desc), C.c_void_p(self.stream)))
+
+    # -- stepping ----------------------------------------------------------
+    def step(self, nsteps, n0=0.0, src_values=None):
+        """Advance ``nsteps`` steps; the first E half-step is at n0 + 1/2.
+
+        ``src_values`` (nsteps, 2, nsrc) overrides the host evaluation of the
+        source-time functions.
+        """
+        nsteps = int(nsteps)
+        done = 0
+        while done < nsteps:
+            k = min(self.src_chunk, nsteps - done)
+            if self.src is not None:
+                vals = (src_values[done:done + k] if src_values is not None else
+                        source_values(self.scene, self.scene.dt, n0 + done, k))
+                # the pinned staging buffer may still be read by the previous
+                # chunk's asynchronous copy
+                if self._staged is not None:
+                    self._staged.synchronize()
+                self.src_host[:k].copy_(_torch().from_numpy(np.ascontiguousarray(vals)))
+                self.src_val[:k].copy_(self.src_host[:k], non_blocking=True)
+                self._staged = _torch().cuda.Event()
+                self._staged.record()
+            N.check(self.lib.gmes_step(C.byref(self.desc), k, C.c_void_p(self.stream)))
+            done += k
+
+    def launch_raw(self, nsteps):
+        """Enqueue ``nsteps`` steps with the source values already staged."""
+        N.check(self.lib.gmes_step(C.byref(self.desc), int(nsteps), C.c_void_p(self.stream)))
+
+    # -- field access ------------------------------------------------------
+    def tensor(self, c):
+        """The raw device tensor of component ``c`` (precision-dependent layout)."""
+        return self.fields[c]
+
+    def read(self, c):
+        """Component ``c`` as a float64 numpy array."""
+        t = self.fields[c]
+        if self.prec == N.DF64:
+            return (t[..., 0].double() + t[..., 1].double()).cpu().numpy()
+        return t.double().cpu().numpy()
+
+    def read_tensor(self, c):
+        """Component ``c`` as a float64 device tensor."""
+        t = self.fields[c]
+        if self.prec == N.DF64:
+            return t[..., 0].double() + t[..., 1].double()
+        return t.double()
+
+    def write(self, c, key, value):
+        torch = _torch()
+        t = self.fields[c]
+        if self.prec == N.DF64:
+            v = torch.as_tensor(value, dtype=torch.float64, device=self.device)
+            hi = v.float()
+            lo = (v - hi.double()).float()
+            t[key + (0,) if isinstance(key, tuple) else (key, Ellipsis, 0)] = hi
+            t[key + (1,) if isinstance(key, tuple) else (key, Ellipsis, 1)] = lo
+        else:
+            t[key] = torch.as_tensor(value, dtype=t.dtype, device=self.device)
+
+    def write_all(self, c, array):
+        torch = _torch()
+        a = torch.as_tensor(np.ascontiguousarray(array, dtype=np.float64), device=self.device)
+        t = self.fields[c]
+        if self.prec == N.DF64:
+            hi = a.float()
+            t[..., 0] = hi
+            t[..., 1] = (a - hi.double()).float()
+        else:
+            t.copy_(a.to(t.dtype))
+
+    def aux_tensor(self, c):
+        """State slots of component ``c`` as a (naux, *shape[, 2]) tensor view."""
+        a = self.aux[c]
+        if a is None:
+            return None
+        torch = _torch()
+        shape = self.scene.shape(c)
+        na = self.desc.naux[c]
+        if self.prec in (N.FP64, N.FP64_STRICT):
+            return a.view(torch.float64).view((na,) + shape)
+        if self.prec == N.FP32:
+            return a.view(torch.float32).view((na,) + shape)
+        return a.view(torch.float32).view((na,) + shape + (2,))
+
+    def synchronize(self):
+        _torch().cuda.synchronize(self.device)

@@ -1,0 +1,240 @@
+/*
+ * gmes_gb300 -- C ABI of the GB300 FDTD time-stepping engine.
+ *
+ * This library replaces the hot path of the GMES electromagnetic solver:
+ * one FDTD time step, i.e. the ghost-plane copies
+ * (gmes/fdtd.py:811-1097), the per-component material updates dispatched
+ * by FDTD.update_ex ... update_hz (gmes/fdtd.py:673-809) to the C++
+ * per-point updaters PwMaterial<T>::update_all (src/pw_material.hh:66-73,
+ * src/pw_dielectric.hh, src/pw_cpml.hh, src/pw_upml.hh, src/pw_drude.hh,
+ * src/pw_lorentz.hh, src/pw_dcp.hh), and the point-source updates
+ * (gmes/pw_source.py:74-131), in the order of FDTD.step()
+ * (gmes/fdtd.py:1099-1122).
+ *
+ * The reference binds one C++ object per (material, component) through
+ * SWIG (src/pw_material.i); each object owns an array-of-structs list of
+ * points with their parameters and state.  Here a grid is described once by
+ *   - a u8 class map per field component (same array shape as the field),
+ *   - a table of update classes with their physical parameters,
+ *   - the PML layers' grading parameters,
+ * and the engine computes every update coefficient from those parameters
+ * in FP64 on the GPU (gmes_build_coefficients).
+ *
+ * Conventions
+ *   - All functions return a gmes_status; 0 is success.  The message of the
+ *     last failure on the calling thread is returned by gmes_last_error().
+ *     The status classes mirror the exception mapping of the reference's
+ *     binding (src/pw_material.i:23-33): bad argument -> ValueError,
+ *     out of range -> IndexError, everything else -> RuntimeError.
+ *   - Every buffer in gmes_grid_desc is DEVICE memory allocated by the
+ *     caller (gmes_grid_sizes() gives the sizes).  The library itself
+ *     allocates no device memory: host inputs are staged through a region
+ *     of the caller's coefficient block.
+ *   - Arrays are C-ordered (k fastest), exactly the reference's numpy
+ *     layout (gmes/geometry.py:276-358).
+ *   - Work is enqueued on the caller's stream (cudaStream_t passed as
+ *     void*; NULL = legacy default stream).  Calls on one grid must not
+ *     overlap on the device.
+ */
+#ifndef GMES_GB300_H_
+#define GMES_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GMES_ABI_VERSION 1
+#define GMES_MAX_CLASSES 256 /* class ids are u8 */
+#define GMES_MAX_PML 4       /* PML materials per grid */
+#define GMES_MAX_POLES 8     /* Drude/Lorentz poles, DCP terms per class */
+
+typedef enum {
+  GMES_OK = 0,
+  GMES_ERR_VALUE = 1,   /* invalid argument (reference: std::invalid_argument) */
+  GMES_ERR_INDEX = 2,   /* index out of range (reference: std::out_of_range) */
+  GMES_ERR_RUNTIME = 3, /* any other failure */
+  GMES_ERR_CUDA = 4     /* a CUDA call failed; the message has the CUDA error */
+} gmes_status;
+
+typedef enum {
+  GMES_FP64 = 0,        /* IEEE FP64 storage and arithmetic, FMA-contracted */
+  GMES_FP32 = 1,        /* FP32 storage and arithmetic, FP64-derived coefficients */
+  GMES_DF64 = 2,        /* float-float pairs (48-bit significand), FP32 pipes */
+  GMES_FP64_STRICT = 3  /* FP64 in the reference's exact operation order, no FMA */
+} gmes_precision;
+
+/* Update kinds (one per reference updater family). */
+typedef enum {
+  GMES_KIND_DUMMY = 0,      /* src/pw_dummy.hh: no update */
+  GMES_KIND_DIELECTRIC = 1, /* src/pw_dielectric.hh */
+  GMES_KIND_CPML = 2,       /* src/pw_cpml.hh */
+  GMES_KIND_UPML = 3,       /* src/pw_upml.hh */
+  GMES_KIND_DRUDE = 4,      /* src/pw_drude.hh (E side; H side is DIELECTRIC) */
+  GMES_KIND_LORENTZ = 5,    /* src/pw_lorentz.hh */
+  GMES_KIND_DCP = 6,        /* src/pw_dcp.hh, DcpAde* (ADE form) */
+  GMES_KIND_CONST = 7       /* src/pw_const.hh */
+} gmes_kind;
+
+/* gmes_grid_desc.flags */
+#define GMES_FLAG_DISPERSIVE 1 /* some E class is DRUDE, LORENTZ or DCP */
+
+/* Field components: bit c of gmes_grid_desc.active. */
+enum { GMES_EX = 0, GMES_EY = 1, GMES_EZ = 2, GMES_HX = 3, GMES_HY = 4, GMES_HZ = 5 };
+
+/*
+ * One update class of one component, with physical parameters
+ * (replaces the per-point <Model>ElectricParam / MagneticParam structs,
+ * src/pw_material.i:215-348).  Parameters live in a double pool:
+ *   DIELECTRIC, CPML, UPML, DUMMY: none
+ *   CONST:   value
+ *   DRUDE:   eps_inf, sigma, then (omega, gamma) per pole   (src/material.pyx:1546-1565)
+ *   LORENTZ: eps_inf, sigma, then (amp, omega, gamma) per pole (src/material.pyx:1727-1746)
+ *   DCP:     eps_inf, sigma, (omega, gamma) per Drude term,
+ *            (amp, cos phi, sin phi, omega, gamma) per critical point
+ *            (src/material.pyx:1074-1105; the phase enters only through
+ *            cos/sin, supplied by the caller's libm)
+ */
+typedef struct {
+  int32_t kind;      /* gmes_kind */
+  int32_t pml;       /* index into the PML list for CPML/UPML, else -1 */
+  int32_t npole;     /* Drude/Lorentz poles, or DCP Drude terms */
+  int32_t ncp;       /* DCP critical points */
+  int32_t param_off; /* first parameter in the parameter pool */
+  int32_t nparam;
+  double eps;        /* eps_inf (E) or mu_inf (H) the update divides by */
+} gmes_class_desc;
+
+/* Grading of one PML material (src/material.pyx:442-502, 558-591, 795-820). */
+typedef struct {
+  int32_t kind;         /* GMES_KIND_CPML or GMES_KIND_UPML */
+  int32_t pad;
+  double sigma_max[3];  /* sigma_max_ratio * sigma_opt, per axis */
+  double m;             /* grading order of sigma and kappa */
+  double kappa_max;
+  double m_a;           /* CPML only: grading order of a */
+  double a_max;         /* CPML only */
+  double d;             /* slab thickness */
+  double center[3];
+  double half_size[3];  /* +inf on an axis whose half size is below d */
+} gmes_pml_desc;
+
+/* One point source, resolved to one Yee point (gmes/pw_source.py:74-131). */
+typedef struct {
+  int32_t comp;   /* field component 0..5 */
+  int32_t mode;   /* 0: field = value (hard); 1: field -= value (current) */
+  int64_t offset; /* linear C-order index into the component's array */
+} gmes_point_source;
+
+/*
+ * The grid: shape, step sizes and the caller-allocated device buffers.
+ * Sizes in bytes of each buffer are given by gmes_grid_sizes().
+ */
+typedef struct {
+  int32_t abi_version;   /* GMES_ABI_VERSION */
+  int32_t precision;     /* gmes_precision */
+  int32_t n[3];          /* Cartesian.whole_field_size */
+  int32_t active;        /* bit c set: component c is updated */
+  int32_t naux[6];       /* state slots per point of component c (see below) */
+  int32_t nclass[6];     /* number of classes of component c */
+  int32_t npml;
+  int32_t nsrc;
+  int32_t nparam;        /* doubles in the class parameter pool */
+  int32_t src_steps;     /* capacity of src_val in steps */
+  int32_t flags;         /* GMES_FLAG_* */
+  int32_t reserved;
+  double dr[3];          /* dx, dy, dz */
+  double half[3];        /* Cartesian.half_size (origin of the Yee coordinates) */
+  double dt;
+  /* device buffers */
+  void* field[6];        /* element type by precision: double, float, float2 */
+  uint8_t* cls[6];       /* class map of each active component */
+  void* aux[6];          /* naux[c] slots x (points of c), same element type */
+  void* coef;            /* coefficient block, written by gmes_build_coefficients */
+  gmes_point_source* src;/* nsrc point sources */
+  double* src_val;       /* source values, [step][source] (see gmes_step) */
+} gmes_grid_desc;
+/*
+ * State slots (naux) per kind, the same state the reference keeps inside
+ * each point's parameter struct:
+ *   CPML 2 (psi1, psi2); UPML 1 (d or b); DRUDE/LORENTZ 2 per pole
+ *   (q_now, q_new); DCP 1 + 2 per Drude term + 2 per critical point
+ *   (e_old, q_old/q_now, p_old/p_now).  naux[c] is the maximum over the
+ *   classes of component c.
+ */
+
+/* Element size in bytes of a field or state value at this precision. */
+int gmes_elem_size(int32_t precision);
+
+/* Array shape of component c (1,1,1 when inactive). */
+gmes_status gmes_field_shape(const gmes_grid_desc* g, int32_t comp, int64_t shape[3]);
+
+/*
+ * Bytes of each device buffer the caller must allocate:
+ *   sizes[0..5]   field[c]        sizes[6..11]  cls[c]
+ *   sizes[12..17] aux[c]          sizes[18]     coef
+ *   sizes[19]     src             sizes[20]     src_val for one step
+ */
+gmes_status gmes_grid_sizes(const gmes_grid_desc* g, int64_t sizes[21]);
+
+/*
+ * Compute every update coefficient in FP64 on the GPU from the class
+ * table, the parameter pool and the PML list, and write the coefficient
+ * block g->coef (replaces Material.init / get_pw_material_* coefficient
+ * assembly, src/material.pyx).  Host arrays: classes[6][nclass[c]]
+ * (component-major, concatenated), params (the pool), pmls[npml].
+ * Synchronous on `stream`.
+ */
+gmes_status gmes_build_coefficients(const gmes_grid_desc* g, const gmes_class_desc* classes,
+                                    const double* params, const gmes_pml_desc* pmls,
+                                    void* stream);
+
+/*
+ * Optional: overwrite the PML profile of (pml, comp, axis) with host values,
+ * for bit-exact comparisons with a CPU implementation whose exp/pow differ
+ * in the last ulp.  values: n = shape[axis] rows of 3 doubles, CPML
+ * (b, c, kappa) or UPML (sigma, kappa, unused); the derived coefficients
+ * are recomputed on the GPU from them.  Synchronous on `stream`.
+ */
+gmes_status gmes_set_pml_profile(const gmes_grid_desc* g, int32_t pml, int32_t comp,
+                                 int32_t axis, const double* values, void* stream);
+
+/*
+ * Read back the FP64 profile of (pml, comp, axis) as computed on the GPU:
+ * shape[axis] rows of 5 doubles, CPML (b, c, kappa, c/d, 1/(kappa d)) or
+ * UPML (c1, c2, c4, c5, c6).  Synchronous on `stream`.
+ */
+gmes_status gmes_get_pml_profile(const gmes_grid_desc* g, int32_t pml, int32_t comp,
+                                 int32_t axis, double* out, void* stream);
+
+/* Zero every field and state buffer (FDTD.init's zero fields). */
+gmes_status gmes_reset(const gmes_grid_desc* g, void* stream);
+
+/*
+ * Advance `nsteps` full time steps starting at step index `step0`
+ * (FDTD.step(), gmes/fdtd.py:1099-1122): H ghost copy, E update, E
+ * sources, E ghost copy, H update, H sources.  Source values are read from
+ * g->src_val: for step s (0-based within this call) the E value of source
+ * q is src_val[(2*s) * nsrc + q] and the H value src_val[(2*s+1) * nsrc + q].
+ */
+gmes_status gmes_step(const gmes_grid_desc* g, int32_t nsteps, void* stream);
+
+/* Copy a component between host and device memory (numpy <-> GPU). */
+gmes_status gmes_read_field(const gmes_grid_desc* g, int32_t comp, double* host_out,
+                            void* stream);
+gmes_status gmes_write_field(const gmes_grid_desc* g, int32_t comp, const double* host_in,
+                             void* stream);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* gmes_last_error(void);
+
+/* GMES_ABI_VERSION of the loaded library. */
+int gmes_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GMES_GB300_H_ */

@@ -1,0 +1,152 @@
+"""Python driver of the CPU oracle (oracle/gmes_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, never by the product package.  The oracle
+consumes the same compiled ``Scene`` as the CUDA engine and restates the
+reference's per-point update loop on the CPU (see the C file's header for
+the reference lines it follows).  Its fidelity is pinned against vectors
+produced by the reference itself (tests/golden/).
+"""
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "gmes_oracle.c"
+BUILD = HERE / "_build"
+LIB = BUILD / "libgmes_oracle.so"
+CFLAGS = ["-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall",
+          "-Wno-unknown-pragmas"]
+
+_lib = None
+
+
+def build():
+    """Compile the oracle with gcc (no FMA contraction: the reference's operation order)."""
+    BUILD.mkdir(exist_ok=True)
+    if LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    tmp = LIB.with_suffix(".so.tmp")
+    subprocess.run(["gcc", *CFLAGS, str(SRC), "-o", str(tmp), "-lm"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    lib = C.CDLL(str(LIB))
+    P = C.POINTER
+    lib.oracle_create.restype = C.c_void_p
+    lib.oracle_create.argtypes = [P(C.c_int), C.c_int, P(C.c_double), P(C.c_double), C.c_double]
+    lib.oracle_add_pml.restype = C.c_int
+    lib.oracle_add_pml.argtypes = [C.c_void_p, C.c_int, P(C.c_double), C.c_double, C.c_double,
+                                   C.c_double, C.c_double, C.c_double, P(C.c_double),
+                                   P(C.c_double)]
+    lib.oracle_add_class.restype = C.c_int
+    lib.oracle_add_class.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                     C.c_int, P(C.c_double), C.c_int]
+    lib.oracle_set_class_map.restype = C.c_int
+    lib.oracle_set_class_map.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8)]
+    lib.oracle_set_sources.restype = C.c_int
+    lib.oracle_set_sources.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int),
+                                       P(C.c_int64)]
+    lib.oracle_field.restype = P(C.c_double)
+    lib.oracle_field.argtypes = [C.c_void_p, C.c_int]
+    lib.oracle_pml_profile.restype = C.c_int
+    lib.oracle_pml_profile.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P(C.c_double)]
+    lib.oracle_step.restype = C.c_int
+    lib.oracle_step.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
+    lib.oracle_threads.restype = C.c_int
+    lib.oracle_destroy.argtypes = [C.c_void_p]
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    """CPU FDTD run of a compiled Scene (FP64, reference operation order)."""
+
+    def __init__(self, scene):
+        from gmes_gb300.scene import class_arrays, source_offsets
+        self.lib = load()
+        self.scene = scene
+        n = (C.c_int * 3)(*scene.n)
+        dr = (C.c_double * 3)(*scene.dr)
+        half = (C.c_double * 3)(*scene.half)
+        self.h = self.lib.oracle_create(n, scene.active_mask, dr, half, scene.dt)
+        if not self.h:
+            raise MemoryError("oracle allocation failed")
+        rows, pool, pmls = class_arrays(scene)
+        for p in pmls:
+            r = self.lib.oracle_add_pml(
+                self.h, p["kind"], (C.c_double * 3)(*p["sigma_max"]), p["m"], p["kappa_max"],
+                p["m_a"], p["a_max"], p["d"], (C.c_double * 3)(*p["center"]),
+                (C.c_double * 3)(*p["half_size"]))
+            if r < 0:
+                raise ValueError("too many PML materials")
+        pool = np.asarray(pool, np.float64) if pool else np.zeros(1)
+        k = 0
+        for c in range(6):
+            for _ in scene.classes[c]:
+                r = rows[k]
+                prm = np.ascontiguousarray(pool[r["param_off"]:r["param_off"] + r["nparam"]])
+                if self.lib.oracle_add_class(self.h, c, r["kind"], r["eps"], r["pml"], r["npole"],
+                                             r["ncp"], _dp(prm), r["nparam"]) < 0:
+                    raise ValueError("bad class")
+                k += 1
+        for c in range(6):
+            if scene.cls[c] is not None:
+                m = np.ascontiguousarray(scene.cls[c], np.uint8)
+                if self.lib.oracle_set_class_map(self.h, c,
+                                                 m.ctypes.data_as(C.POINTER(C.c_uint8))) != 0:
+                    raise ValueError("bad class map")
+        srcs = source_offsets(scene)
+        comp = (C.c_int * max(1, len(srcs)))(*[s[0] for s in srcs])
+        mode = (C.c_int * max(1, len(srcs)))(*[s[1] for s in srcs])
+        off = (C.c_int64 * max(1, len(srcs)))(*[s[2] for s in srcs])
+        self.lib.oracle_set_sources(self.h, len(srcs), comp, mode, off)
+        self.n = 0.0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.oracle_destroy(self.h)
+            self.h = None
+
+    def step(self, nsteps, src_values=None):
+        from gmes_gb300.scene import source_values
+        if src_values is None:
+            src_values = source_values(self.scene, self.scene.dt, self.n, nsteps)
+        v = np.ascontiguousarray(src_values, np.float64)
+        if v.size == 0:
+            v = np.zeros(1)
+        self.lib.oracle_step(self.h, int(nsteps), _dp(v))
+        self.n += nsteps
+
+    def field(self, c):
+        sh = self.scene.shape(c)
+        ptr = self.lib.oracle_field(self.h, c)
+        return np.ctypeslib.as_array(ptr, shape=sh).copy()
+
+    def fields(self):
+        return [self.field(c) for c in range(6)]
+
+    def pml_profile(self, pml, c, axis):
+        n = self.scene.shape(c)[axis]
+        out = np.zeros((n, 3), np.float64)
+        if self.lib.oracle_pml_profile(self.h, pml, c, axis, _dp(out)) != 0:
+            raise IndexError("bad pml index")
+        return out
+
+    @staticmethod
+    def threads():
+        return load().oracle_threads()

@@ -1,0 +1,155 @@
+"""Scene builders shared by the golden-vector generator and the tests.
+
+Each builder takes a module exposing GMES's public API -- the reference
+``gmes`` package (fixture generation in the build container) or
+``gmes_gb300`` (tests) -- and returns ``(sim, nsteps)``.  Geometry and
+parameters are seeded so both sides build exactly the same scene.
+"""
+
+import numpy as np
+
+
+def tmz_regression(g):
+    """tests/test_fdtd.py:55-79 of the reference: TMz + CPML + Continuous Ez, 5 steps."""
+    space = g.Cartesian(size=(2, 2, 0), resolution=5)
+    geometry = [g.DefaultMedium(material=g.Dielectric()), g.Shell(material=g.Cpml())]
+    sources = [g.PointSource(src_time=g.Continuous(freq=0.8, width=0.5), center=(0, 0, 0),
+                             component=g.Ez)]
+    return g.TMzFDTD(space, geometry, sources, verbose=False), 5
+
+
+def air2d(g):
+    """examples/air2d.py: 200x200 TMz, vacuum + 20-cell CPML, Continuous(0.8) Ez, to t = 10."""
+    space = g.Cartesian(size=(10, 10, 0), resolution=20)
+    geometry = [g.DefaultMedium(material=g.Dielectric()), g.Shell(material=g.Cpml())]
+    sources = [g.PointSource(src_time=g.Continuous(freq=0.8), center=(0, 0, 0), component=g.Ez)]
+    return g.TMzFDTD(space, geometry, sources, verbose=False), 286
+
+
+def random_objects(g, rng, n, half, rmin, rmax, dx, eps_lo=1.0, eps_hi=12.0):
+    """Seeded spheres and blocks (50/50), radius / half-edge in [rmin, rmax] cells."""
+    objs = []
+    for _ in range(n):
+        r = rng.uniform(rmin, rmax) * dx
+        center = tuple(float(v) for v in rng.uniform(-half, half, 3))
+        eps = float(rng.uniform(eps_lo, eps_hi))
+        if rng.uniform() < 0.5:
+            objs.append(g.Sphere(material=g.Dielectric(eps_inf=eps), center=center, radius=r))
+        else:
+            objs.append(g.Block(material=g.Dielectric(eps_inf=eps), center=center,
+                                size=(2 * r, 2 * r, 2 * r)))
+    return objs
+
+
+def dielectric3d(g, size=2.0, res=10, pml_cells=4, nobj=5, seed=0, steps=150):
+    """Small instance of the 256^3 benchmark scene: seeded dielectric spheres and
+    blocks, CPML on all faces, Bandpass Ex point source."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / res
+    inner = size / 2 - pml_cells * dx
+    space = g.Cartesian(size=(size, size, size), resolution=res)
+    geometry = [g.DefaultMedium(material=g.Dielectric())]
+    geometry += random_objects(g, rng, nobj, inner * 0.7, 2, 5, dx)
+    geometry.append(g.Shell(material=g.Cpml(), thickness=pml_cells * dx))
+    sources = [g.PointSource(src_time=g.Bandpass(freq=0.5, fwidth=1.0), center=(0, 0, 0),
+                             component=g.Ex)]
+    return g.FDTD(space, geometry, sources, verbose=False), steps
+
+
+def dispersive3d(g, size=2.0, res=10, pml_cells=4, seed=1, steps=150, courant_ratio=0.6):
+    """Small instance of the 192^3 dispersive scene: eps = 2.25 background, a
+    Drude sphere, a Lorentz slab, a DCP-ADE sphere, UPML on all faces.
+
+    The reference derives dt from the background medium (gmes/fdtd.py:132-147):
+    with eps = 2.25 the default Courant ratio 0.99 exceeds the stability limit
+    of every eps < 2.25 region (eps_inf = 1 metal), so the scene runs at
+    courant_ratio 0.6 (< 0.99 / 1.5)."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / res
+    space = g.Cartesian(size=(size, size, size), resolution=res)
+    cps = tuple(g.CriticalPoint(amp=float(rng.uniform(0.5, 2.0)),
+                                phi=float(rng.uniform(-1.5, 1.5)),
+                                omega=float(rng.uniform(2.0, 5.0)),
+                                gamma=float(rng.uniform(0.2, 1.0))) for _ in range(2))
+    geometry = [
+        g.DefaultMedium(material=g.Dielectric(eps_inf=2.25)),
+        g.Sphere(material=g.Drude(eps_inf=1, dps=(g.DrudePole(omega=9.0, gamma=0.07),)),
+                 center=(-0.35, -0.3, 0.2), radius=0.3),
+        g.Block(material=g.Lorentz(lps=(g.LorentzPole(amp=2.0, omega=3.0, gamma=0.1),)),
+                center=(0.3, 0.0, 0.0), size=(0.2, 1.2, 1.2)),
+        g.Sphere(material=g.DcpAde(eps_inf=1.1, dps=(g.DrudePole(omega=7.0, gamma=0.2),),
+                                   cps=cps), center=(-0.2, 0.35, -0.3), radius=0.25),
+        g.Shell(material=g.Upml(), thickness=pml_cells * dx),
+    ]
+    sources = [g.PointSource(src_time=g.Bandpass(freq=0.5, fwidth=1.0), center=(0, 0, 0),
+                             component=g.Ez)]
+    return g.FDTD(space, geometry, sources, verbose=False,
+                  courant_ratio=courant_ratio), steps
+
+
+def drude2d(g, steps=120):
+    """TMz Drude medium (omega 1, gamma 0.1) with a dielectric slab running into the
+    CPML (the PML's underneath eps differs from the background)."""
+    space = g.Cartesian(size=(3, 3, 0), resolution=12)
+    geometry = [
+        g.DefaultMedium(material=g.Drude(dps=(g.DrudePole(omega=1.0, gamma=0.1),))),
+        g.Block(material=g.Dielectric(eps_inf=4.0), center=(0, 0.6, 0), size=(10, 0.5, 1)),
+        g.Shell(material=g.Cpml(), thickness=0.5),
+    ]
+    sources = [g.PointSource(src_time=g.Bandpass(freq=0.8, fwidth=1.0), center=(0.1, -0.2, 0),
+                             component=g.Ez)]
+    return g.TMzFDTD(space, geometry, sources, verbose=False), steps
+
+
+def tez_upml_currents(g, steps=100):
+    """TEz (Ex, Ey, Hz) with UPML, an electric-current (Jx) and a magnetic-current
+    (Mz) source, DifferentiatedGaussian and Continuous time functions."""
+    space = g.Cartesian(size=(2.5, 2, 0), resolution=12)
+    geometry = [
+        g.DefaultMedium(material=g.Dielectric(eps_inf=1.5, mu_inf=1.2)),
+        g.Cylinder(material=g.Dielectric(eps_inf=6.0), center=(0.3, 0.1, 0), radius=0.3,
+                   height=2),
+        g.Shell(material=g.Upml(), thickness=0.4),
+    ]
+    sources = [
+        g.PointSource(src_time=g.DifferentiatedGaussian(tw=0.3, t0=1.0), center=(-0.2, 0, 0),
+                      component=g.Jx, amp=2.0),
+        g.PointSource(src_time=g.Continuous(freq=1.2, width=0.8), center=(0.2, -0.3, 0),
+                      component=g.Mz),
+    ]
+    return g.TEzFDTD(space, geometry, sources, verbose=False), steps
+
+
+def tmx_cpml_hard(g, steps=80):
+    """TMx (Ex; Hy, Hz), x collapsed, CPML, an Ellipsoid, a hard Hy source."""
+    space = g.Cartesian(size=(0, 2.4, 2), resolution=10)
+    geometry = [
+        g.DefaultMedium(material=g.Dielectric()),
+        g.Ellipsoid(material=g.Dielectric(eps_inf=3.0), center=(0, 0.2, -0.1),
+                    size=(1, 0.8, 0.5)),
+        g.Shell(material=g.Cpml(), thickness=0.5),
+    ]
+    sources = [
+        g.PointSource(src_time=g.Bandpass(freq=1.0, fwidth=1.5), center=(0, -0.3, 0.2),
+                      component=g.Ex),
+        g.PointSource(src_time=g.Continuous(freq=0.7, width=0.5), center=(0, 0.4, 0.1),
+                      component=g.Hy, amp=0.5),
+    ]
+    return g.TMxFDTD(space, geometry, sources, verbose=False), steps
+
+
+CASES = {
+    "tmz_regression": tmz_regression,
+    "air2d": air2d,
+    "dielectric3d": dielectric3d,
+    "dispersive3d": dispersive3d,
+    "drude2d": drude2d,
+    "tez_upml_currents": tez_upml_currents,
+    "tmx_cpml_hard": tmx_cpml_hard,
+}
+
+# Cases whose golden file stores only Ez in full (and checksums of the rest)
+# to keep the fixture small.
+SUMMARY_ONLY = {"air2d": ("ez",)}
+
+COMP_NAMES = ("ex", "ey", "ez", "hx", "hy", "hz")

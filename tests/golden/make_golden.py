@@ -1,0 +1,65 @@
+"""Generate the golden vectors in tests/golden/ by running the REFERENCE.
+
+Runs the reference GMES package (built by ``oracle/build_ref.py`` from the
+reference checkout, which exists only in the build container) on every case
+of ``cases.py`` and stores the resulting fields with the reference's time
+bookkeeping.  The tests compare the CPU oracle and the CUDA engine against
+these files; they never need the reference itself.
+
+Usage:  python tests/golden/make_golden.py [case ...]
+"""
+
+import json
+import os
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(HERE))
+
+from cases import CASES, COMP_NAMES, SUMMARY_ONLY  # noqa: E402
+
+
+def checksum(a):
+    a = np.asarray(a, np.float64)
+    return [float(np.sum(a)), float(np.sum(a * a)), float(np.max(np.abs(a)))]
+
+
+def main(names):
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from oracle.refpkg import load_reference
+    gmes = load_reference()
+    for name in names:
+        t0 = time.time()
+        sim, nsteps = CASES[name](gmes)
+        sim.init()
+        t1 = time.time()
+        for _ in range(nsteps):
+            sim.step()
+        t2 = time.time()
+        keep = SUMMARY_ONLY.get(name, COMP_NAMES)
+        arrays = {}
+        meta = {"case": name, "steps": nsteps, "n": sim.time_step.n, "t": sim.time_step.t,
+                "dt": sim.time_step.dt, "shapes": {}, "checksums": {},
+                "updaters": {}, "init_s": t1 - t0, "step_s": t2 - t1}
+        for comp in COMP_NAMES:
+            f = np.asarray(getattr(sim, comp))
+            meta["shapes"][comp] = list(f.shape)
+            meta["checksums"][comp] = checksum(f)
+            if comp in keep:
+                arrays[comp] = f
+        for comp, ups in sim.pw_material.items():
+            meta["updaters"][comp.__name__] = {type(u).__name__: int(u.idx_size())
+                                               for u in ups.values()}
+        np.savez_compressed(HERE / f"{name}.npz", **arrays)
+        (HERE / f"{name}.json").write_text(json.dumps(meta, indent=1, sort_keys=True) + "\n")
+        print(f"{name}: init {t1 - t0:.1f}s, {nsteps} steps {t2 - t1:.1f}s", flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:] or list(CASES))

@@ -1,0 +1,107 @@
+"""The C ABI library: loads, exports what include/gmes_gb300.h declares, and
+validates descriptors on the host (no GPU needed for these calls)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+from gmes_gb300 import _native as N
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "gmes_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gmes_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_function():
+    lib = N.load()
+    names = declared_functions()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(lib, name), f"{name} declared in gmes_gb300.h but not exported"
+    assert sorted(N.EXPORTS) == names
+
+
+def test_abi_version_and_elem_sizes():
+    lib = N.load()
+    assert lib.gmes_abi_version() == N.ABI_VERSION
+    assert [lib.gmes_elem_size(p) for p in (N.FP64, N.FP32, N.DF64, N.FP64_STRICT)] == [8, 4, 8, 8]
+    assert lib.gmes_elem_size(9) == 0
+
+
+def _desc(**kw):
+    d = N.GridDescC()
+    d.abi_version = N.ABI_VERSION
+    d.precision = kw.get("precision", N.FP64)
+    for a in range(3):
+        d.n[a] = kw.get("n", (4, 5, 6))[a]
+        d.dr[a] = 0.1
+    d.dt = 0.05
+    d.active = kw.get("active", 63)
+    for c in range(6):
+        d.nclass[c] = 2
+        d.naux[c] = 2
+    d.npml = kw.get("npml", 1)
+    return d
+
+
+def test_grid_sizes_match_reference_shapes():
+    lib = N.load()
+    d = _desc()
+    sizes = (C.c_int64 * 21)()
+    N.check(lib.gmes_grid_sizes(C.byref(d), sizes))
+    shapes = [(4, 6, 7), (5, 5, 7), (5, 6, 6), (4, 6, 7), (5, 5, 7), (5, 6, 6)]
+    for c, sh in enumerate(shapes):
+        np_ = sh[0] * sh[1] * sh[2]
+        assert sizes[c] == 8 * np_
+        assert sizes[6 + c] == np_
+        assert sizes[12 + c] == 2 * 8 * np_
+        s = (C.c_int64 * 3)()
+        N.check(lib.gmes_field_shape(C.byref(d), c, s))
+        assert tuple(s) == sh
+    assert sizes[18] > 0 and sizes[18] % 256 == 0
+
+
+def test_inactive_components_are_one_point():
+    lib = N.load()
+    d = _desc(active=0b110100)  # TMz: Ez, Hx, Hy
+    s = (C.c_int64 * 3)()
+    N.check(lib.gmes_field_shape(C.byref(d), 0, s))
+    assert tuple(s) == (1, 1, 1)
+    N.check(lib.gmes_field_shape(C.byref(d), 2, s))
+    assert tuple(s) == (5, 6, 6)
+
+
+@pytest.mark.parametrize("field,value,exc", [
+    ("abi_version", 99, ValueError),
+    ("precision", 7, ValueError),
+    ("active", 0b000111, ValueError),
+    ("npml", 9, ValueError),
+])
+def test_descriptor_validation(field, value, exc):
+    lib = N.load()
+    d = _desc()
+    setattr(d, field, value)
+    sizes = (C.c_int64 * 21)()
+    with pytest.raises(exc):
+        N.check(lib.gmes_grid_sizes(C.byref(d), sizes))
+    assert lib.gmes_last_error()
+
+
+def test_bad_component_index():
+    lib = N.load()
+    d = _desc()
+    s = (C.c_int64 * 3)()
+    with pytest.raises(IndexError):
+        N.check(lib.gmes_field_shape(C.byref(d), 6, s))
+
+
+def test_step_rejects_null_buffers_without_touching_the_gpu():
+    lib = N.load()
+    d = _desc()
+    with pytest.raises(ValueError, match="NULL"):
+        N.check(lib.gmes_step(C.byref(d), 1, None))

@@ -1,0 +1,124 @@
+"""CUDA engine against the reference's own vectors and the CPU oracle.
+
+Tolerances (relative L2 per field component against the FP64 reference):
+  fp64_strict  bit-exact (reference operation order, host PML profiles)
+  fp64         <= 1e-12 (FMA-contracted, reciprocals precomputed)
+  df64         <= 1e-12 (float-float pairs)
+  fp32         <= 2e-3  (FP32 storage and arithmetic; error stated, not bounded by the reference)
+"""
+import numpy as np
+import pytest
+
+import gmes_gb300 as G
+from cases import CASES, COMP_NAMES
+from conftest import load_golden, rel_l2
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "df64": 1e-12, "fp32": 2e-3}
+
+
+def run_case(name, precision, host_profiles=False):
+    sim, nsteps = CASES[name](G)
+    sim.precision = precision
+    sim.init()
+    if host_profiles:
+        orc = Oracle(sim.scene)
+        for p in range(len(sim.scene.pmls)):
+            for comp in sim.scene.active:
+                for axis in range(3):
+                    sim.engine.set_pml_profile(p, comp.index, axis,
+                                               orc.pml_profile(p, comp.index, axis))
+    sim.step_until_n(nsteps)
+    return sim, nsteps
+
+
+_oracle_cache = {}
+
+
+def oracle_fields(name):
+    if name not in _oracle_cache:
+        sim, n = CASES[name](G)
+        orc = Oracle(sim.compile())
+        orc.step(n)
+        _oracle_cache[name] = orc.fields()
+    return _oracle_cache[name]
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_strict_is_bit_exact_with_reference(name):
+    sim, _ = run_case(name, "fp64_strict", host_profiles=True)
+    gold, _ = load_golden(name)
+    ref = oracle_fields(name)
+    for c, cn in enumerate(COMP_NAMES):
+        f = sim.field[G.constant.COMPONENTS[c]].numpy()
+        if cn in gold:
+            assert np.array_equal(f, gold[cn]), (name, cn, rel_l2(f, gold[cn]))
+        assert np.array_equal(f, ref[c]), (name, cn, rel_l2(f, ref[c]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "df64", "fp32"])
+@pytest.mark.parametrize("name", list(CASES))
+def test_fast_modes_within_tolerance(name, precision):
+    sim, _ = run_case(name, precision)
+    ref = oracle_fields(name)
+    for c, cn in enumerate(COMP_NAMES):
+        f = sim.field[G.constant.COMPONENTS[c]].numpy()
+        assert f.shape == ref[c].shape
+        assert np.isfinite(f).all()
+        err = rel_l2(f, ref[c])
+        assert err <= TOL[precision], (name, precision, cn, err)
+
+
+def test_gpu_profiles_match_host_libm():
+    """PML profiles computed in FP64 on the GPU agree with host libm to 1e-12."""
+    for name in ("dielectric3d", "dispersive3d"):
+        sim, _ = CASES[name](G)
+        sim.init()
+        orc = Oracle(sim.scene)
+        upml = name == "dispersive3d"
+        for comp in sim.scene.active:
+            for axis in range(3):
+                host = orc.pml_profile(0, comp.index, axis)
+                dev = sim.engine.get_pml_profile(0, comp.index, axis)
+                if upml:  # host gives (sigma, kappa); compare c1 = (2k - s dt)/(2k + s dt)
+                    dt = sim.scene.dt
+                    s_, k_ = host[:, 0], host[:, 1]
+                    host = np.stack([(2 * k_ - s_ * dt) / (2 * k_ + s_ * dt),
+                                     2 * dt / (2 * k_ + s_ * dt), 1 / (2 * k_ + s_ * dt)], 1)
+                np.testing.assert_allclose(dev[:, :3], host, rtol=1e-12, atol=1e-300)
+
+
+def test_public_api_roundtrip():
+    """init/step/field write-through as in the reference's tests/test_fdtd.py:20-53."""
+    space = G.Cartesian(size=(2, 2, 0), resolution=3)
+    sim = G.TMzFDTD(space=space, geom_list=[G.DefaultMedium(material=G.Dielectric())],
+                    verbose=False)
+    sim.init()
+    sim.step()
+    assert sim.src_list == [] and sim.time_step.n == 1
+    for field in sim.field.values():
+        assert not field.any()
+    sim2 = G.TMzFDTD(space=G.Cartesian(size=(2, 2, 0), resolution=3),
+                     geom_list=[G.DefaultMedium(material=G.Dielectric())], verbose=False)
+    sim2.init()
+    idx = sim2.space.space_to_ez_index(0, 0, 0)
+    sim2.ez[idx] = 1
+    assert sim2.ez[idx] == 1
+    sim2.step_while_zero(G.Ez, (0, 0, 0))
+    assert sim2.time_step.n == 1
+    with pytest.raises(ValueError, match="outside the simulation domain"):
+        sim2.step_while_zero(G.Ez, (100, 100, 100))
+
+
+def test_deepcopy_continues_identically():
+    import copy
+    sim, _ = CASES["drude2d"](G)
+    sim.init()
+    sim.step_until_n(20)
+    twin = copy.deepcopy(sim)
+    sim.step_until_n(40)
+    twin.step_until_n(40)
+    for comp in G.constant.COMPONENTS:
+        np.testing.assert_array_equal(sim.field[comp].numpy(), twin.field[comp].numpy())
