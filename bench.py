@@ -1,0 +1,420 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FDTD engine on the benchmark scenes.
+
+Default workload: the 3-D dielectric + CPML scene on a 256^3 grid (24 seeded
+spheres/blocks, eps in [1, 12], 10-cell CPML, Bandpass Ex point source),
+FP64.  One benchmark step = one full FDTD time step (E and H half-steps) of
+the whole grid.  Prints ONE JSON line (rank 0).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload cube|dispersive|air2d] [--n 256] [--precision fp64]
+
+Multi-GPU (torchrun, one process per GPU): the grid does not split across
+GPUs in this engine, so every rank advances its own replica of the scene
+(weak scaling); value = cells * steps summed over ranks / max rank time.
+
+``--impl reference`` times the CPU oracle (a C restatement of the
+reference's OpenMP per-point update loop, oracle/gmes_oracle.c) on the host
+cores, on the same scene: the reference's own build (Cython + SWIG) cannot
+be built on the GPU host.
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gcell-updates/s & HBM GB/s vs 8 TB/s; batched p50/p99 job latency"
+UNIT = "Gcell-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", choices=("cube", "dispersive", "air2d"), default="cube")
+    ap.add_argument("--n", type=int, default=None, help="grid side (cube 256, dispersive 192)")
+    ap.add_argument("--precision", default="fp64",
+                    choices=("fp64", "df64", "fp32", "fp64_strict"))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="target length of the CPU-baseline sample")
+    ap.add_argument("--quiet-extras", action="store_true",
+                    help="only the timed loop (for profiling runs)")
+    return ap.parse_args()
+
+
+def build_sim(args, precision):
+    from gmes_gb300 import workloads as W
+    if args.workload == "cube":
+        n = args.n or 256
+        sim, full_steps = W.cube(n=n, precision=precision)
+        cfg = {"workload": f"cube{n}_dielectric_cpml", "grid": [n, n, n], "objects": 24,
+               "pml_cells": 10, "source": "Bandpass(0.5, 0.2) Ex point", "job_steps": full_steps}
+    elif args.workload == "dispersive":
+        n = args.n or 192
+        sim, full_steps = W.dispersive(n=n, precision=precision)
+        cfg = {"workload": f"cube{n}_drude_lorentz_dcp_upml", "grid": [n, n, n],
+               "pml_cells": 12, "source": "Bandpass(0.5, 0.2) Ez point (TFSF pending)",
+               "courant_ratio": 0.6, "job_steps": full_steps}
+    else:
+        sim, full_steps = W.air2d(precision=precision)
+        cfg = {"workload": "air2d_tmz_200x200_cpml", "grid": [200, 200, 1],
+               "source": "Continuous(0.8) Ez point", "job_steps": full_steps}
+    return sim, cfg
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "of measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "of fallback"
+
+
+def ncu_traffic(workload_key, precision):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        data = json.loads(p.read_text())
+        return data.get(f"{workload_key}/{precision}")
+    except ValueError:
+        return None
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes
+# ---------------------------------------------------------------------------
+def half_bytes(scene, precision):
+    """Algorithmic DRAM bytes of each half-step: (E half, H half).
+
+    E half: read+write every E value, read every H value, read the E class
+    ids, read+write the E state slots of the points that carry state
+    (CPML psi, UPML d, ADE q/p).  H half symmetric.
+    """
+    from gmes_gb300.scene import naux_of
+    es = 4 if precision == "fp32" else 8
+    out = []
+    for side in (0, 1):
+        b = 0
+        for comp in scene.active:
+            c = comp.index
+            npts = int(np.prod(scene.shape(c)))
+            if (c < 3) == (side == 0):
+                b += 2 * es * npts + npts
+                for cid, cnt in scene.counts(c).items():
+                    b += 2 * naux_of(scene.classes[c][cid]) * es * cnt
+            else:
+                b += es * npts
+        out.append(b)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# our engine
+# ---------------------------------------------------------------------------
+def timed_loop(sim, steps, warmup, rank_sync):
+    import torch
+    eng = sim.engine
+    chunk = eng.src_chunk
+    # warm-up (untimed)
+    done = 0
+    n0 = 0.0
+    while done < warmup:
+        k = min(chunk, warmup - done)
+        eng.stage_sources(n0 + done, k)
+        for s in range(k):
+            eng.half_step(0, s)
+            eng.half_step(1, s)
+        done += k
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    # stage the first chunk of source values before the clock starts
+    base = float(warmup)
+    eng.stage_sources(base, min(chunk, steps))
+    torch.cuda.synchronize()
+    rank_sync()
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    t_start.record()
+    for s in range(steps):
+        slot = s % chunk
+        if slot == 0 and s > 0:
+            eng.stage_sources(base + s, min(chunk, steps - s))
+        a, b, c = ev[s]
+        a.record()
+        eng.half_step(0, slot)
+        b.record()
+        eng.half_step(1, slot)
+        c.record()
+    t_end.record()
+    torch.cuda.synchronize()
+    rank_sync()
+    wall = time.perf_counter() - t0
+    total_ms = t_start.elapsed_time(t_end)
+    e_ms = sum(a.elapsed_time(b) for a, b, _ in ev) / steps
+    h_ms = sum(b.elapsed_time(c) for _, b, c in ev) / steps
+    return total_ms, e_ms, h_ms, wall
+
+
+def e2e_loop(sim, steps):
+    """Same metric through the public API: sim.step() per step (host source
+    evaluation + pinned H2D copy of the step's source values) and a D2H read
+    of the probe value at the source point each step."""
+    import torch
+    scene = sim.scene
+    src = scene.sources[0] if scene.sources else None
+    c = src.comp.index if src else scene.active[0].index
+    idx = src.idx if src else (0, 0, 0)
+    field = sim.engine.fields[c]
+    probe = torch.empty((1,) + tuple(field.shape[3:]), dtype=field.dtype).pin_memory()
+    for _ in range(3):
+        sim.step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+        probe.copy_(field[idx].reshape(probe.shape), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    wall = time.perf_counter() - t0
+    h2d = 2 * len(scene.sources) * 8
+    d2h = probe.numel() * probe.element_size()
+    return wall, h2d, d2h
+
+
+def cpu_baseline(sim, seconds, threads=None):
+    """Time the CPU oracle on a bounded number of steps of the same scene."""
+    from oracle.oracle import Oracle
+    t0 = time.perf_counter()
+    orc = Oracle(sim.scene)
+    setup = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    orc.step(1)
+    one = time.perf_counter() - t1
+    nsteps = max(1, min(200, int(seconds / max(one, 1e-6))))
+    t2 = time.perf_counter()
+    orc.step(nsteps)
+    dt = time.perf_counter() - t2
+    cells = sim.scene.cells
+    return {"value": cells * nsteps / dt / 1e9, "unit": UNIT, "cores": Oracle.threads(),
+            "kind": "port",
+            "sample": (f"{nsteps} FDTD steps of the same scene after 1 warm-up step "
+                       f"(point-list setup {setup:.1f}s excluded), C oracle with OpenMP "
+                       f"static loops, {Oracle.threads()} threads")}, nsteps, dt
+
+
+def run_ours(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def rank_sync():
+        if dist is not None:
+            dist.barrier()
+
+    sim, cfg = build_sim(args, args.precision)
+    sim.init()
+    scene = sim.scene
+    cells = scene.cells
+    clk = ClockSampler(local)
+    clk.start()
+    total_ms, e_ms, h_ms, wall = timed_loop(sim, args.steps, args.warmup, rank_sync)
+    clocks = clk.stop()
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = cells * args.steps * world / (total_ms / 1e3) / 1e9
+    eb, hb = half_bytes(scene, args.precision)
+    dom = ("E half-step", eb, e_ms) if e_ms >= h_ms else ("H half-step", hb, h_ms)
+    peak, peak_src = measured_peak()
+    achieved = dom[1] / (dom[2] / 1e3) / 1e9
+    step_bytes = eb + hb
+    key = f"{cfg['workload']}/{args.precision}"
+    traffic = ncu_traffic(key, args.precision)
+    result = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp64_strict": "f64", "fp32": "f32",
+                  "df64": "df64 (f32 pair)"}[args.precision],
+        "data": "synthetic (seeded scene, no dataset)",
+        "config": dict(cfg, precision=args.precision, parallelism=f"replicas x{world}",
+                       cells=cells, l2="inputs larger than L2 (fields alone "
+                       f"{sum(t.numel() * t.element_size() for t in sim.engine.fields) / 1e6:.0f} MB)"),
+        "hbm_gbs_alg": round(step_bytes / (total_ms / args.steps / 1e3) / 1e9, 1),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "kernel": dom[0], "alg_bytes_per_launch": dom[1],
+                     "launch_ms": round(dom[2], 5), "peak_source": peak_src},
+        "half_ms": {"E": round(e_ms, 5), "H": round(h_ms, 5)},
+        "gpu_launches": args.steps * (6 if scene.sources else 4),
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.quiet_extras:
+        if not args.no_variants and args.precision == "fp64" and world == 1:
+            result["variants"] = {}
+            del sim
+            torch.cuda.empty_cache()
+            for prec in ("df64", "fp32"):
+                vs, _ = build_sim(args, prec)
+                vs.init()
+                vk = min(args.steps, 100)
+                t_ms, ve, vh, _ = timed_loop(vs, vk, 5, lambda: None)
+                veb, vhb = half_bytes(vs.scene, prec)
+                vdom = (veb, ve) if ve >= vh else (vhb, vh)
+                result["variants"][prec] = {
+                    "value": round(cells * vk / (t_ms / 1e3) / 1e9, 4),
+                    "ms_per_step": round(t_ms / vk, 5),
+                    "roofline_frac": round(vdom[0] / (vdom[1] / 1e3) / 1e9 / peak, 4)}
+                del vs
+                torch.cuda.empty_cache()
+            sim, _ = build_sim(args, args.precision)
+            sim.init()
+        if not args.no_e2e:
+            k = max(1, min(args.steps, 200))
+            wall_e2e, h2d, d2h = e2e_loop(sim, k)
+            result["e2e"] = {"value": round(cells * k * world / wall_e2e / 1e9, 4), "unit": UNIT,
+                             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                             "api": "FDTD.step() + probe read, host source values"}
+        if not args.no_cpu_baseline and world == 1:
+            cb, _, _ = cpu_baseline(sim, args.cpu_seconds)
+            result["cpu_baseline"] = cb
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def run_reference(args):
+    """CPU reference arm: the oracle port on all host cores, same scene and metric."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    sim, cfg = build_sim(args, "fp64")
+    scene = sim.compile()
+    from oracle.oracle import Oracle
+    t0 = time.perf_counter()
+    orc = Oracle(scene)
+    setup = time.perf_counter() - t0
+    w = max(1, min(args.warmup, 3))
+    tw = time.perf_counter()
+    orc.step(w)
+    per_step = (time.perf_counter() - tw) / w
+    # bound the timed CPU work to about a minute
+    k = max(1, min(args.steps, int(60.0 / max(per_step, 1e-6))))
+    t1 = time.perf_counter()
+    orc.step(k)
+    dt = time.perf_counter() - t1
+    value = scene.cells * k / dt / 1e9
+    result = {
+        "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": 0,
+        "steps": k, "warmup": w, "ms_per_step": round(dt / k * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded scene, no dataset)", "impl": "reference",
+        "config": dict(cfg, precision="fp64", parallelism="host cores"),
+        "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": Oracle.threads(),
+                         "kind": "port",
+                         "sample": (f"{k} of the requested {args.steps} steps "
+                                    f"(bounded to ~60 s), setup {setup:.1f}s excluded")},
+        "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(result), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

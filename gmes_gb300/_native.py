@@ -23,7 +23,7 @@ EXPORTS = [
     "gmes_abi_version", "gmes_last_error", "gmes_elem_size", "gmes_field_shape",
     "gmes_grid_sizes", "gmes_build_coefficients", "gmes_set_pml_profile",
     "gmes_get_pml_profile", "gmes_reset",
-    "gmes_step", "gmes_read_field", "gmes_write_field",
+    "gmes_step", "gmes_half_step", "gmes_read_field", "gmes_write_field",
 ]
 
 
@@ -89,6 +89,7 @@ def load():
                                          P(C.c_double), C.c_void_p]
     lib.gmes_reset.argtypes = [P(GridDescC), C.c_void_p]
     lib.gmes_step.argtypes = [P(GridDescC), C.c_int32, C.c_void_p]
+    lib.gmes_half_step.argtypes = [P(GridDescC), C.c_int32, C.c_int32, C.c_void_p]
     lib.gmes_read_field.argtypes = [P(GridDescC), C.c_int32, P(C.c_double), C.c_void_p]
     lib.gmes_write_field.argtypes = [P(GridDescC), C.c_int32, P(C.c_double), C.c_void_p]
     for name in EXPORTS:

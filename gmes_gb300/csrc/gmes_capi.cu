@@ -94,6 +94,7 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
   for (int a = 0; a < 3; ++a) {
     d.n[a] = g.n[a];
     d.dr[a] = g.dr[a];
+    d.rdr[a] = make_coef(1.0 / g.dr[a]);
   }
   d.dt = g.dt;
   d.active = g.active;
@@ -338,6 +339,19 @@ gmes_status gmes_step(const gmes_grid_desc* g, int32_t nsteps, void* stream) {
   const GridDev d = make_grid_dev(*g);
   cudaError_t e = launch_step(*g, d, nsteps, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching step kernels");
+  return GMES_OK;
+}
+
+gmes_status gmes_half_step(const gmes_grid_desc* g, int32_t side, int32_t step, void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  if (side != 0 && side != 1) return fail(GMES_ERR_VALUE, "side = %d must be 0 (E) or 1 (H)", side);
+  if (step < 0 || (g->nsrc > 0 && step >= g->src_steps))
+    return fail(GMES_ERR_INDEX, "step %d outside the source-value buffer (%d steps)", step,
+                g->src_steps);
+  const GridDev d = make_grid_dev(*g);
+  cudaError_t e = launch_half(*g, d, side, step, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching half-step kernels");
   return GMES_OK;
 }
 

@@ -140,6 +140,7 @@ struct GridDev {
   const double* src_val;
   double dr[3];
   double dt;
+  Coef rdr[3];            // 1 / dr, computed on the host
 };
 
 // ---------------------------------------------------------------------------
@@ -233,6 +234,8 @@ GridDev make_grid_dev(const gmes_grid_desc& g);
 
 // Launchers implemented per precision in gmes_step.cu.
 cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps,
+                        cudaStream_t s);
+cudaError_t launch_half(const gmes_grid_desc& g, const GridDev& d, int side, int step,
                         cudaStream_t s);
 cudaError_t launch_build_coefficients(const gmes_grid_desc& g, const GridDev& d,
                                       cudaStream_t s);

@@ -26,6 +26,7 @@ namespace gmes {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kIChunk = 16;  // cells per thread along i in k_march
 
 template <int C>
 __device__ __forceinline__ int64_t stride_of(const GridDev& g, int axis) {
@@ -73,8 +74,8 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
     P::st(fp, E ? F + cdt * X : F - cdt * X);
     return;
   }
-  const R r1 = P::from_double(1.0 / g.dr[a1]);
-  const R r2 = P::from_double(1.0 / g.dr[a2]);
+  const R r1 = P::cf(g.rdr[a1]);
+  const R r2 = P::cf(g.rdr[a2]);
   if (kind == GMES_KIND_UPML) {
     const Coef* q1 = g.prof[cc.pml][C][a1] + (int64_t)x[a1] * kProfStride;
     const Coef* q2 = g.prof[cc.pml][C][a2] + (int64_t)x[a2] * kProfStride;
@@ -357,11 +358,12 @@ __device__ __forceinline__ void cell_h(const GridDev& g, int i, int j, int k) {
 
 template <class P, int SIDE, bool STRICT, bool DISP>
 __global__ void __launch_bounds__(kThreads) k_half(const GridDev g, int i0) {
-  const int64_t plane = (int64_t)g.n[1] * g.n[2];
-  const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  // plane = n1 * n2 < 2^31 (checked by the host)
+  const int plane = g.n[1] * g.n[2];
+  const int t = blockIdx.x * kThreads + threadIdx.x;
   if (t >= plane) return;
-  const int j = (int)(t / g.n[2]);
-  const int k = (int)(t - (int64_t)j * g.n[2]);
+  const int j = t / g.n[2];
+  const int k = t - j * g.n[2];
   const int i = i0 + (int)blockIdx.y;
   if (i >= g.n[0]) return;
   if constexpr (SIDE == 0) {
@@ -372,6 +374,93 @@ __global__ void __launch_bounds__(kThreads) k_half(const GridDev g, int i0) {
     if (g.active & 8) cell_h<P, 3, STRICT, DISP>(g, i, j, k);
     if (g.active & 16) cell_h<P, 4, STRICT, DISP>(g, i, j, k);
     if (g.active & 32) cell_h<P, 5, STRICT, DISP>(g, i, j, k);
+  }
+}
+
+// Column-marching form of the half-step for grids with n2 >= 32: a block of
+// 32 x 8 threads covers a (k, j) tile and every thread walks a run of
+// `ichunk` cells along i.  The value of the previous i plane that the curl
+// needs (Hz and Hy for the E half, Ez and Ey for the H half) is carried in
+// registers, so each cell loads 7 neighbour values instead of 9 and no index
+// is divided.  In-plane offsets are 32-bit; the i offset is 64-bit.
+template <class P, int C>
+__device__ __forceinline__ typename P::R ldc(const GridDev& g, int64_t off) {
+  if (!(g.active & (1 << C))) return P::zero();
+  return P::ld(static_cast<const typename P::T*>(g.f[C]) + off);
+}
+
+template <class P, int C, bool STRICT, bool DISP>
+__device__ __forceinline__ void upd(const GridDev& g, int64_t lin, int x0, int x1, int x2,
+                                    typename P::R p1, typename P::R p2) {
+  if (!(g.active & (1 << C))) return;
+  const int x[3] = {x0, x1, x2};
+  if constexpr (STRICT)
+    update_strict<C, DISP>(g, lin, x, p1, p2);
+  else
+    update_fast<P, C, DISP>(g, lin, x, p1, p2);
+}
+
+template <class P, int SIDE, bool STRICT, bool DISP>
+__global__ void __launch_bounds__(256) k_march(const GridDev g, int ichunk) {
+  using R = typename P::R;
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int ibeg = blockIdx.z * ichunk;
+  if (k >= g.n[2] || j >= g.n[1] || ibeg >= g.n[0]) return;
+  const int iend = min(ibeg + ichunk, g.n[0]);
+  // per-component strides (axis 2 stride is 1)
+  const int64_t sx0 = g.st[0][0], sy0 = g.st[1][0], sz0 = g.st[2][0];
+  const int64_t hx0 = g.st[3][0], hy0 = g.st[4][0], hz0 = g.st[5][0];
+  const int sx1 = (int)g.st[0][1], sy1 = (int)g.st[1][1], sz1 = (int)g.st[2][1];
+  const int hx1 = (int)g.st[3][1], hy1 = (int)g.st[4][1], hz1 = (int)g.st[5][1];
+  if constexpr (SIDE == 0) {
+    // E half.  Hz[i, j+1, k] and Hy[i, j, k+1] carried along i.
+    R hz_prev = ldc<P, 5>(g, (int64_t)ibeg * hz0 + (j + 1) * hz1 + k);
+    R hy_prev = ldc<P, 4>(g, (int64_t)ibeg * hy0 + j * hy1 + k + 1);
+    for (int i = ibeg; i < iend; ++i) {
+      const int64_t hzb = (int64_t)(i + 1) * hz0 + j * hz1 + k;  // Hz[i+1, j, k]
+      const int64_t hyb = (int64_t)(i + 1) * hy0 + j * hy1 + k;  // Hy[i+1, j, k]
+      const int64_t hxb = (int64_t)i * hx0 + j * hx1 + k;        // Hx[i, j, k]
+      const R hz_a = ldc<P, 5>(g, hzb + hz1);                    // Hz[i+1, j+1, k]
+      const R hz_b = ldc<P, 5>(g, hzb);
+      const R hy_a = ldc<P, 4>(g, hyb + 1);                      // Hy[i+1, j, k+1]
+      const R hy_b = ldc<P, 4>(g, hyb);
+      const R hx_a = ldc<P, 3>(g, hxb + hx1 + 1);                // Hx[i, j+1, k+1]
+      const R hx_b = ldc<P, 3>(g, hxb + hx1);                    // Hx[i, j+1, k]
+      const R hx_c = ldc<P, 3>(g, hxb + 1);                      // Hx[i, j, k+1]
+      upd<P, 0, STRICT, DISP>(g, (int64_t)i * sx0 + j * sx1 + k, i, j, k, hz_a - hz_b,
+                              hy_a - hy_b);
+      upd<P, 1, STRICT, DISP>(g, (int64_t)i * sy0 + j * sy1 + k, i, j, k, hx_a - hx_b,
+                              hz_a - hz_prev);
+      upd<P, 2, STRICT, DISP>(g, (int64_t)i * sz0 + j * sz1 + k, i, j, k, hy_a - hy_prev,
+                              hx_a - hx_c);
+      hz_prev = hz_a;
+      hy_prev = hy_a;
+    }
+  } else {
+    // H half.  Ez[i, j, k] and Ey[i, j, k] carried along i.
+    R ez_cur = ldc<P, 2>(g, (int64_t)ibeg * sz0 + j * sz1 + k);
+    R ey_cur = ldc<P, 1>(g, (int64_t)ibeg * sy0 + j * sy1 + k);
+    for (int i = ibeg; i < iend; ++i) {
+      const int64_t ezb = (int64_t)i * sz0 + j * sz1 + k;
+      const int64_t eyb = (int64_t)i * sy0 + j * sy1 + k;
+      const int64_t exb = (int64_t)i * sx0 + j * sx1 + k;
+      const R ez_n = ldc<P, 2>(g, ezb + sz0);      // Ez[i+1, j, k]
+      const R ez_j = ldc<P, 2>(g, ezb + sz1);      // Ez[i, j+1, k]
+      const R ey_n = ldc<P, 1>(g, eyb + sy0);      // Ey[i+1, j, k]
+      const R ey_k = ldc<P, 1>(g, eyb + 1);        // Ey[i, j, k+1]
+      const R ex_0 = ldc<P, 0>(g, exb);            // Ex[i, j, k]
+      const R ex_k = ldc<P, 0>(g, exb + 1);        // Ex[i, j, k+1]
+      const R ex_j = ldc<P, 0>(g, exb + sx1);      // Ex[i, j+1, k]
+      upd<P, 3, STRICT, DISP>(g, (int64_t)i * hx0 + (j + 1) * hx1 + k + 1, i, j + 1, k + 1,
+                              ez_j - ez_cur, ey_k - ey_cur);
+      upd<P, 4, STRICT, DISP>(g, (int64_t)(i + 1) * hy0 + j * hy1 + k + 1, i + 1, j, k + 1,
+                              ex_k - ex_0, ez_n - ez_cur);
+      upd<P, 5, STRICT, DISP>(g, (int64_t)(i + 1) * hz0 + (j + 1) * hz1 + k, i + 1, j + 1, k,
+                              ey_n - ey_cur, ex_j - ex_0);
+      ez_cur = ez_n;
+      ey_cur = ey_n;
+    }
   }
 }
 
@@ -437,9 +526,10 @@ __global__ void k_sources(const GridDev g, int side, int64_t slot) {
   }
 }
 
+// One half-step: ghost copy of the other half's components, the fused
+// update of this half's components, this half's point sources.
 template <class P, bool STRICT>
-cudaError_t run_steps(const gmes_grid_desc& g, const GridDev& d, int nsteps, cudaStream_t s,
-                      bool disp) {
+void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp) {
   using T = typename P::T;
   const int64_t plane = (int64_t)d.n[1] * d.n[2];
   const unsigned bx = (unsigned)((plane + kThreads - 1) / kThreads);
@@ -451,44 +541,79 @@ cudaError_t run_steps(const gmes_grid_desc& g, const GridDev& d, int nsteps, cud
         maxplane = v > maxplane ? v : maxplane;
       }
   const dim3 ggrid((unsigned)((maxplane + 255) / 256), 6);
-  const int srcblocks = d.nsrc > 0 ? (d.nsrc + 127) / 128 : 0;
   constexpr int kMaxY = 65535;
-  for (int st = 0; st < nsteps; ++st) {
-    k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1, maxplane);
-    for (int i0 = 0; i0 < d.n[0]; i0 += kMaxY) {
-      const dim3 grid(bx, (unsigned)min(kMaxY, d.n[0] - i0));
+  k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
+  if (d.n[2] >= 32) {
+    const dim3 grid((unsigned)((d.n[2] + 31) / 32), (unsigned)((d.n[1] + 7) / 8),
+                    (unsigned)((d.n[0] + kIChunk - 1) / kIChunk));
+    const dim3 block(32, 8);
+    if (side == 0) {
       if (disp)
-        k_half<P, 0, STRICT, true><<<grid, kThreads, 0, s>>>(d, i0);
+        k_march<P, 0, STRICT, true><<<grid, block, 0, s>>>(d, kIChunk);
       else
-        k_half<P, 0, STRICT, false><<<grid, kThreads, 0, s>>>(d, i0);
+        k_march<P, 0, STRICT, false><<<grid, block, 0, s>>>(d, kIChunk);
+    } else {
+      k_march<P, 1, STRICT, false><<<grid, block, 0, s>>>(d, kIChunk);
     }
-    if (srcblocks) k_sources<P, STRICT><<<srcblocks, 128, 0, s>>>(d, 0, 2 * (int64_t)st);
-    k_ghost<T><<<ggrid, 256, 0, s>>>(d, 0, maxplane);
+  } else {
     for (int i0 = 0; i0 < d.n[0]; i0 += kMaxY) {
       const dim3 grid(bx, (unsigned)min(kMaxY, d.n[0] - i0));
-      k_half<P, 1, STRICT, false><<<grid, kThreads, 0, s>>>(d, i0);
+      if (side == 0) {
+        if (disp)
+          k_half<P, 0, STRICT, true><<<grid, kThreads, 0, s>>>(d, i0);
+        else
+          k_half<P, 0, STRICT, false><<<grid, kThreads, 0, s>>>(d, i0);
+      } else {
+        k_half<P, 1, STRICT, false><<<grid, kThreads, 0, s>>>(d, i0);
+      }
     }
-    if (srcblocks) k_sources<P, STRICT><<<srcblocks, 128, 0, s>>>(d, 1, 2 * (int64_t)st + 1);
+  }
+  if (d.nsrc > 0)
+    k_sources<P, STRICT><<<(d.nsrc + 127) / 128, 128, 0, s>>>(d, side, 2 * (int64_t)st + side);
+}
+
+template <class P, bool STRICT>
+cudaError_t run_steps(const GridDev& d, int nsteps, int side_mask, int st0, cudaStream_t s,
+                      bool disp) {
+  for (int st = 0; st < nsteps; ++st) {
+    if (side_mask & 1) run_half<P, STRICT>(d, 0, st0 + st, s, disp);
+    if (side_mask & 2) run_half<P, STRICT>(d, 1, st0 + st, s, disp);
   }
   return cudaGetLastError();
+}
+
+template <class P, bool STRICT>
+cudaError_t dispatch(const gmes_grid_desc& g, const GridDev& d, int nsteps, int side_mask,
+                     int st0, cudaStream_t s) {
+  const bool disp = (g.flags & GMES_FLAG_DISPERSIVE) != 0;
+  return run_steps<P, STRICT>(d, nsteps, side_mask, st0, s, disp);
+}
+
+cudaError_t dispatch_precision(const gmes_grid_desc& g, const GridDev& d, int nsteps,
+                               int side_mask, int st0, cudaStream_t s) {
+  switch (g.precision) {
+    case GMES_FP64:
+      return dispatch<PolF64, false>(g, d, nsteps, side_mask, st0, s);
+    case GMES_FP64_STRICT:
+      return dispatch<PolF64, true>(g, d, nsteps, side_mask, st0, s);
+    case GMES_FP32:
+      return dispatch<PolF32, false>(g, d, nsteps, side_mask, st0, s);
+    case GMES_DF64:
+      return dispatch<PolDF, false>(g, d, nsteps, side_mask, st0, s);
+    default:
+      return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace
 
 cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps, cudaStream_t s) {
-  const bool disp = (g.flags & GMES_FLAG_DISPERSIVE) != 0;
-  switch (g.precision) {
-    case GMES_FP64:
-      return run_steps<PolF64, false>(g, d, nsteps, s, disp);
-    case GMES_FP64_STRICT:
-      return run_steps<PolF64, true>(g, d, nsteps, s, disp);
-    case GMES_FP32:
-      return run_steps<PolF32, false>(g, d, nsteps, s, disp);
-    case GMES_DF64:
-      return run_steps<PolDF, false>(g, d, nsteps, s, disp);
-    default:
-      return cudaErrorInvalidValue;
-  }
+  return dispatch_precision(g, d, nsteps, 3, 0, s);
+}
+
+cudaError_t launch_half(const gmes_grid_desc& g, const GridDev& d, int side, int step,
+                        cudaStream_t s) {
+  return dispatch_precision(g, d, 1, side == 0 ? 1 : 2, step, s);
 }
 
 }  // namespace gmes

@@ -180,6 +180,25 @@ class GridEngine:
             N.check(self.lib.gmes_step(C.byref(self.desc), k, C.c_void_p(self.stream)))
             done += k
 
+    def half_step(self, side, slot=0):
+        """Enqueue one half-step (0: E, 1: H) reading staged source slot ``slot``."""
+        N.check(self.lib.gmes_half_step(C.byref(self.desc), int(side), int(slot),
+                                        C.c_void_p(self.stream)))
+
+    def stage_sources(self, n0, nsteps):
+        """Stage the source values of ``nsteps`` steps from time step n0 (<= src_chunk)."""
+        if self.src is None:
+            return
+        if nsteps > self.src_chunk:
+            raise ValueError("more steps than the staging buffer holds")
+        vals = source_values(self.scene, self.scene.dt, n0, nsteps)
+        if self._staged is not None:
+            self._staged.synchronize()
+        self.src_host[:nsteps].copy_(_torch().from_numpy(vals))
+        self.src_val[:nsteps].copy_(self.src_host[:nsteps], non_blocking=True)
+        self._staged = _torch().cuda.Event()
+        self._staged.record()
+
     def launch_raw(self, nsteps):
         """Enqueue ``nsteps`` steps with the source values already staged."""
         N.check(self.lib.gmes_step(C.byref(self.desc), int(nsteps), C.c_void_p(self.stream)))

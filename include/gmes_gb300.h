@@ -221,6 +221,13 @@ gmes_status gmes_reset(const gmes_grid_desc* g, void* stream);
  */
 gmes_status gmes_step(const gmes_grid_desc* g, int32_t nsteps, void* stream);
 
+/*
+ * One half of step `step` (0-based index into src_val, < src_steps when
+ * there are sources): side 0 = H ghost copy, E update, E sources; side 1 =
+ * E ghost copy, H update, H sources.  gmes_step(g, n) is n pairs of these.
+ */
+gmes_status gmes_half_step(const gmes_grid_desc* g, int32_t side, int32_t step, void* stream);
+
 /* Copy a component between host and device memory (numpy <-> GPU). */
 gmes_status gmes_read_field(const gmes_grid_desc* g, int32_t comp, double* host_out,
                             void* stream);
