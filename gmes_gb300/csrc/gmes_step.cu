@@ -26,7 +26,10 @@ namespace gmes {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kIChunk = 16;  // cells per thread along i in k_march
+#ifndef GMES_MIN_BLOCKS
+#define GMES_MIN_BLOCKS 4
+#endif
+constexpr int kMinBlocks = GMES_MIN_BLOCKS;  // resident blocks per SM the register budget targets
 
 template <int C>
 __device__ __forceinline__ int64_t stride_of(const GridDev& g, int axis) {
@@ -39,20 +42,41 @@ __device__ __forceinline__ int64_t stride_of(const GridDev& g, int axis) {
 //   side 0 (E): F += c1 D1 - c2 D2            (Dielectric E)
 //   side 1 (H): F += c2 D2 - c1 D1            (Dielectric H)
 // ---------------------------------------------------------------------------
+// State values of a CPML (psi1, psi2) or UPML (d) point, loaded for all
+// three components of a cell before any of them is computed.
+template <class P>
+struct Pre {
+  typename P::R a, b;
+};
+
+template <class P, int C>
+__device__ __forceinline__ Pre<P> prefetch_state(const GridDev& g, int64_t lin, uint8_t id) {
+  Pre<P> r{P::zero(), P::zero()};
+  if (!(g.active & (1 << C))) return r;
+  const int kind = g.tab[C][id].kind;
+  const typename P::T* aux = static_cast<const typename P::T*>(g.aux[C]);
+  if (kind == GMES_KIND_CPML) {
+    r.a = P::ldw(aux + lin);
+    r.b = P::ldw(aux + g.npts[C] + lin);
+  } else if (kind == GMES_KIND_UPML) {
+    r.a = P::ldw(aux + lin);
+  }
+  return r;
+}
+
 template <class P, int C, bool DISP>
 __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const int x[3],
-                                            typename P::R p1, typename P::R p2) {
+                                            typename P::R p1, typename P::R p2,
+                                            typename P::R F, uint8_t id, Pre<P> pre) {
   using R = typename P::R;
   using T = typename P::T;
   constexpr int own = C % 3, a1 = (own + 1) % 3, a2 = (own + 2) % 3;
   constexpr bool E = C < 3;
-  const uint8_t id = g.cls[C][lin];
   const ClassCoef& cc = g.tab[C][id];
   const int kind = cc.kind;
   if (kind == GMES_KIND_DUMMY) return;
   T* fp = static_cast<T*>(g.f[C]) + lin;
   if (kind == GMES_KIND_DIELECTRIC) {
-    const R F = P::ldw(fp);
     const R c1 = P::cf(cc.c1), c2 = P::cf(cc.c2);
     P::st(fp, E ? (F + c1 * p1) - c2 * p2 : (F + c2 * p2) - c1 * p1);
     return;
@@ -64,12 +88,11 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
     const Coef* q2 = g.prof[cc.pml][C][a2] + (int64_t)x[a2] * kProfStride;
     T* s1 = aux + lin;
     T* s2 = aux + np + lin;
-    const R psi1 = P::cf(q1[0]) * P::ldw(s1) + P::cf(q1[3]) * p1;
-    const R psi2 = P::cf(q2[0]) * P::ldw(s2) + P::cf(q2[3]) * p2;
+    const R psi1 = P::cf(q1[0]) * pre.a + P::cf(q1[3]) * p1;
+    const R psi2 = P::cf(q2[0]) * pre.b + P::cf(q2[3]) * p2;
     P::st(s1, psi1);
     P::st(s2, psi2);
     const R X = (P::cf(q1[4]) * p1 - P::cf(q2[4]) * p2) + (psi1 - psi2);
-    const R F = P::ldw(fp);
     const R cdt = P::cf(cc.cdt);
     P::st(fp, E ? F + cdt * X : F - cdt * X);
     return;
@@ -81,12 +104,11 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
     const Coef* q2 = g.prof[cc.pml][C][a2] + (int64_t)x[a2] * kProfStride;
     const Coef* q3 = g.prof[cc.pml][C][own] + (int64_t)x[own] * kProfStride;
     T* sp = aux + lin;
-    const R d_old = P::ldw(sp);
+    const R d_old = pre.a;
     const R curl = p1 * r1 - p2 * r2;
     const R d_new = E ? P::cf(q1[0]) * d_old + P::cf(q1[1]) * curl
                       : P::cf(q1[0]) * d_old - P::cf(q1[1]) * curl;
     P::st(sp, d_new);
-    const R F = P::ldw(fp);
     P::st(fp, P::cf(q2[0]) * F +
                   P::cf(q2[2]) * (P::cf(q3[3]) * d_new - P::cf(q3[4]) * d_old) *
                       P::cf(cc.reps));
@@ -99,7 +121,7 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
   if constexpr (DISP && E) {
     const Coef* pool = g.pool[C] + (int64_t)id * kPoolStride;
     const R curl = p1 * r1 - p2 * r2;
-    const R e_now = P::ldw(fp);
+    const R e_now = F;
     if (kind == GMES_KIND_DRUDE || kind == GMES_KIND_LORENTZ) {
       // src/pw_drude.hh:89-151, src/pw_lorentz.hh:96-157
       R sum = P::zero();
@@ -177,10 +199,9 @@ __device__ __forceinline__ double DIV(double a, double b) { return __ddiv_rn(a, 
 
 template <int C, bool DISP>
 __device__ __forceinline__ void update_strict(const GridDev& g, int64_t lin, const int x[3],
-                                              double D1, double D2) {
+                                              double D1, double D2, double F, uint8_t id) {
   constexpr int own = C % 3, a1 = (own + 1) % 3, a2 = (own + 2) % 3;
   constexpr bool E = C < 3;
-  const uint8_t id = g.cls[C][lin];
   const ClassCoef& cc = g.tab[C][id];
   const int kind = cc.kind;
   if (kind == GMES_KIND_DUMMY) return;
@@ -189,7 +210,7 @@ __device__ __forceinline__ void update_strict(const GridDev& g, int64_t lin, con
   if (kind == GMES_KIND_DIELECTRIC) {
     // E: e += dt/eps * (D1/d1 - D2/d2); H: h += dt/mu * (D2/d2 - D1/d1)
     const double X = E ? SUB(DIV(D1, d1), DIV(D2, d2)) : SUB(DIV(D2, d2), DIV(D1, d1));
-    *fp = ADD(*fp, MUL(DIV(dt, eps), X));
+    *fp = ADD(F, MUL(DIV(dt, eps), X));
     return;
   }
   double* aux = static_cast<double*>(g.aux[C]);
@@ -207,7 +228,7 @@ __device__ __forceinline__ void update_strict(const GridDev& g, int64_t lin, con
     const double X =
         SUB(ADD(SUB(DIV(DIV(D1, d1), q1[2].d), DIV(DIV(D2, d2), q2[2].d)), psi1), psi2);
     const double inc = MUL(DIV(dt, eps), X);
-    *fp = E ? ADD(*fp, inc) : SUB(*fp, inc);
+    *fp = E ? ADD(F, inc) : SUB(F, inc);
     return;
   }
   const double curl = SUB(DIV(D1, d1), DIV(D2, d2));
@@ -221,7 +242,7 @@ __device__ __forceinline__ void update_strict(const GridDev& g, int64_t lin, con
     const double dn = E ? ADD(MUL(q1[0].d, dstore), MUL(q1[1].d, curl))
                         : SUB(MUL(q1[0].d, dstore), MUL(q1[1].d, curl));
     *sp = dn;
-    *fp = ADD(MUL(q2[0].d, *fp),
+    *fp = ADD(MUL(q2[0].d, F),
               DIV(MUL(q2[2].d, SUB(MUL(q3[3].d, dn), MUL(q3[4].d, dstore))), eps));
     return;
   }
@@ -231,7 +252,7 @@ __device__ __forceinline__ void update_strict(const GridDev& g, int64_t lin, con
   }
   if constexpr (DISP && E) {
     const Coef* pool = g.pool[C] + (int64_t)id * kPoolStride;
-    const double e_now = *fp;
+    const double e_now = F;
     if (kind == GMES_KIND_DRUDE || kind == GMES_KIND_LORENTZ) {
       double sum = 0.0;
       for (int q = 0; q < cc.npole; ++q) {
@@ -300,167 +321,111 @@ __device__ __forceinline__ void update_strict(const GridDev& g, int64_t lin, con
   }
 }
 
-// E component C at cell (i, j, k).
-template <class P, int C, bool STRICT, bool DISP>
-__device__ __forceinline__ void cell_e(const GridDev& g, int i, int j, int k) {
-  using R = typename P::R;
-  using T = typename P::T;
-  constexpr int own = C, a1 = (own + 1) % 3, a2 = (own + 2) % 3;
-  constexpr int in1 = 3 + a2, in2 = 3 + a1;
-  const int x[3] = {i, j, k};
-  const int64_t lin = (int64_t)i * g.st[C][0] + (int64_t)j * g.st[C][1] + k;
-  R p1 = P::zero(), p2 = P::zero();
-  if (g.active & (1 << in1)) {
-    const T* h = static_cast<const T*>(g.f[in1]);
-    const int64_t b = (int64_t)i * g.st[in1][0] + (int64_t)j * g.st[in1][1] + k +
-                      stride_of<in1>(g, own);
-    p1 = P::ld(h + b + stride_of<in1>(g, a1)) - P::ld(h + b);
-  }
-  if (g.active & (1 << in2)) {
-    const T* h = static_cast<const T*>(g.f[in2]);
-    const int64_t b = (int64_t)i * g.st[in2][0] + (int64_t)j * g.st[in2][1] + k +
-                      stride_of<in2>(g, own);
-    p2 = P::ld(h + b + stride_of<in2>(g, a2)) - P::ld(h + b);
-  }
-  if constexpr (STRICT)
-    update_strict<C, DISP>(g, lin, x, p1, p2);
-  else
-    update_fast<P, C, DISP>(g, lin, x, p1, p2);
-}
-
-// H component C (3..5) at cell (i, j, k) = point (i, j, k) + e_a1 + e_a2.
-template <class P, int C, bool STRICT, bool DISP>
-__device__ __forceinline__ void cell_h(const GridDev& g, int i, int j, int k) {
-  using R = typename P::R;
-  using T = typename P::T;
-  constexpr int own = C - 3, a1 = (own + 1) % 3, a2 = (own + 2) % 3;
-  constexpr int in1 = a2, in2 = a1;
-  int x[3] = {i, j, k};
-  x[a1] += 1;
-  x[a2] += 1;
-  const int64_t lin = (int64_t)x[0] * g.st[C][0] + (int64_t)x[1] * g.st[C][1] + x[2];
-  R p1 = P::zero(), p2 = P::zero();
-  if (g.active & (1 << in1)) {
-    const T* e = static_cast<const T*>(g.f[in1]);
-    const int64_t b = (int64_t)i * g.st[in1][0] + (int64_t)j * g.st[in1][1] + k;
-    p1 = P::ld(e + b + stride_of<in1>(g, a1)) - P::ld(e + b);
-  }
-  if (g.active & (1 << in2)) {
-    const T* e = static_cast<const T*>(g.f[in2]);
-    const int64_t b = (int64_t)i * g.st[in2][0] + (int64_t)j * g.st[in2][1] + k;
-    p2 = P::ld(e + b + stride_of<in2>(g, a2)) - P::ld(e + b);
-  }
-  if constexpr (STRICT)
-    update_strict<C, DISP>(g, lin, x, p1, p2);
-  else
-    update_fast<P, C, DISP>(g, lin, x, p1, p2);
-}
-
-template <class P, int SIDE, bool STRICT, bool DISP>
-__global__ void __launch_bounds__(kThreads) k_half(const GridDev g, int i0) {
-  // plane = n1 * n2 < 2^31 (checked by the host)
-  const int plane = g.n[1] * g.n[2];
-  const int t = blockIdx.x * kThreads + threadIdx.x;
-  if (t >= plane) return;
-  const int j = t / g.n[2];
-  const int k = t - j * g.n[2];
-  const int i = i0 + (int)blockIdx.y;
-  if (i >= g.n[0]) return;
-  if constexpr (SIDE == 0) {
-    if (g.active & 1) cell_e<P, 0, STRICT, DISP>(g, i, j, k);
-    if (g.active & 2) cell_e<P, 1, STRICT, DISP>(g, i, j, k);
-    if (g.active & 4) cell_e<P, 2, STRICT, DISP>(g, i, j, k);
-  } else {
-    if (g.active & 8) cell_h<P, 3, STRICT, DISP>(g, i, j, k);
-    if (g.active & 16) cell_h<P, 4, STRICT, DISP>(g, i, j, k);
-    if (g.active & 32) cell_h<P, 5, STRICT, DISP>(g, i, j, k);
-  }
-}
-
-// Column-marching form of the half-step for grids with n2 >= 32: a block of
-// 32 x 8 threads covers a (k, j) tile and every thread walks a run of
-// `ichunk` cells along i.  The value of the previous i plane that the curl
-// needs (Hz and Hy for the E half, Ez and Ey for the H half) is carried in
-// registers, so each cell loads 7 neighbour values instead of 9 and no index
-// is divided.  In-plane offsets are 32-bit; the i offset is 64-bit.
+// ---------------------------------------------------------------------------
+// The half-step kernel.  One thread per cell (i, j, k) of the N0 x N1 x N2
+// update domain; the thread updates the three components of its half there.
+// Every value the cell needs from DRAM -- the class ids, the component's own
+// values and the nine neighbour values of the curls -- is loaded up front,
+// before any store, so a thread waits for one memory latency instead of a
+// chain of them; only state slots (PML, ADE) are loaded after the class is
+// known.  Block = bx x by threads over (k, j) with bx = min(32, n2 rounded up
+// to a power of two), so thin (2-D) grids still fill whole warps along j;
+// grid.z walks i.
+// ---------------------------------------------------------------------------
 template <class P, int C>
-__device__ __forceinline__ typename P::R ldc(const GridDev& g, int64_t off) {
+__device__ __forceinline__ typename P::R ldf(const GridDev& g, int64_t off) {
   if (!(g.active & (1 << C))) return P::zero();
   return P::ld(static_cast<const typename P::T*>(g.f[C]) + off);
 }
 
+template <int C>
+__device__ __forceinline__ uint8_t ldc(const GridDev& g, int64_t off) {
+  if (!(g.active & (1 << C))) return 0;
+  return __ldg(g.cls[C] + off);
+}
+
 template <class P, int C, bool STRICT, bool DISP>
 __device__ __forceinline__ void upd(const GridDev& g, int64_t lin, int x0, int x1, int x2,
-                                    typename P::R p1, typename P::R p2) {
+                                    typename P::R p1, typename P::R p2, typename P::R F,
+                                    uint8_t id, Pre<P> pre) {
   if (!(g.active & (1 << C))) return;
   const int x[3] = {x0, x1, x2};
   if constexpr (STRICT)
-    update_strict<C, DISP>(g, lin, x, p1, p2);
+    update_strict<C, DISP>(g, lin, x, p1, p2, F, id);
   else
-    update_fast<P, C, DISP>(g, lin, x, p1, p2);
+    update_fast<P, C, DISP>(g, lin, x, p1, p2, F, id, pre);
+}
+
+template <class P, int C, bool STRICT>
+__device__ __forceinline__ Pre<P> pre_of(const GridDev& g, int64_t lin, uint8_t id) {
+  if constexpr (STRICT) {
+    return Pre<P>{P::zero(), P::zero()};
+  } else {
+    return prefetch_state<P, C>(g, lin, id);
+  }
 }
 
 template <class P, int SIDE, bool STRICT, bool DISP>
-__global__ void __launch_bounds__(256) k_march(const GridDev g, int ichunk) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_cell(const GridDev g, int bx_log2, int i0) {
   using R = typename P::R;
-  const int k = blockIdx.x * 32 + threadIdx.x;
-  const int j = blockIdx.y * 8 + threadIdx.y;
-  const int ibeg = blockIdx.z * ichunk;
-  if (k >= g.n[2] || j >= g.n[1] || ibeg >= g.n[0]) return;
-  const int iend = min(ibeg + ichunk, g.n[0]);
-  // per-component strides (axis 2 stride is 1)
-  const int64_t sx0 = g.st[0][0], sy0 = g.st[1][0], sz0 = g.st[2][0];
-  const int64_t hx0 = g.st[3][0], hy0 = g.st[4][0], hz0 = g.st[5][0];
-  const int sx1 = (int)g.st[0][1], sy1 = (int)g.st[1][1], sz1 = (int)g.st[2][1];
-  const int hx1 = (int)g.st[3][1], hy1 = (int)g.st[4][1], hz1 = (int)g.st[5][1];
+  const int bx = 1 << bx_log2;
+  const int tx = threadIdx.x & (bx - 1);
+  const int ty = threadIdx.x >> bx_log2;
+  const int k = blockIdx.x * bx + tx;
+  const int j = blockIdx.y * (kThreads >> bx_log2) + ty;
+  const int i = i0 + (int)blockIdx.z;
+  if (k >= g.n[2] || j >= g.n[1] || i >= g.n[0]) return;
   if constexpr (SIDE == 0) {
-    // E half.  Hz[i, j+1, k] and Hy[i, j, k+1] carried along i.
-    R hz_prev = ldc<P, 5>(g, (int64_t)ibeg * hz0 + (j + 1) * hz1 + k);
-    R hy_prev = ldc<P, 4>(g, (int64_t)ibeg * hy0 + j * hy1 + k + 1);
-    for (int i = ibeg; i < iend; ++i) {
-      const int64_t hzb = (int64_t)(i + 1) * hz0 + j * hz1 + k;  // Hz[i+1, j, k]
-      const int64_t hyb = (int64_t)(i + 1) * hy0 + j * hy1 + k;  // Hy[i+1, j, k]
-      const int64_t hxb = (int64_t)i * hx0 + j * hx1 + k;        // Hx[i, j, k]
-      const R hz_a = ldc<P, 5>(g, hzb + hz1);                    // Hz[i+1, j+1, k]
-      const R hz_b = ldc<P, 5>(g, hzb);
-      const R hy_a = ldc<P, 4>(g, hyb + 1);                      // Hy[i+1, j, k+1]
-      const R hy_b = ldc<P, 4>(g, hyb);
-      const R hx_a = ldc<P, 3>(g, hxb + hx1 + 1);                // Hx[i, j+1, k+1]
-      const R hx_b = ldc<P, 3>(g, hxb + hx1);                    // Hx[i, j+1, k]
-      const R hx_c = ldc<P, 3>(g, hxb + 1);                      // Hx[i, j, k+1]
-      upd<P, 0, STRICT, DISP>(g, (int64_t)i * sx0 + j * sx1 + k, i, j, k, hz_a - hz_b,
-                              hy_a - hy_b);
-      upd<P, 1, STRICT, DISP>(g, (int64_t)i * sy0 + j * sy1 + k, i, j, k, hx_a - hx_b,
-                              hz_a - hz_prev);
-      upd<P, 2, STRICT, DISP>(g, (int64_t)i * sz0 + j * sz1 + k, i, j, k, hy_a - hy_prev,
-                              hx_a - hx_c);
-      hz_prev = hz_a;
-      hy_prev = hy_a;
-    }
+    // own points: Ex, Ey, Ez at (i, j, k)
+    const int64_t lx = (int64_t)i * g.st[0][0] + (j * g.st[0][1] + k);
+    const int64_t ly = (int64_t)i * g.st[1][0] + (j * g.st[1][1] + k);
+    const int64_t lz = (int64_t)i * g.st[2][0] + (j * g.st[2][1] + k);
+    const uint8_t idx = ldc<0>(g, lx), idy = ldc<1>(g, ly), idz = ldc<2>(g, lz);
+    const R ex = ldf<P, 0>(g, lx), ey = ldf<P, 1>(g, ly), ez = ldf<P, 2>(g, lz);
+    // neighbour H values
+    const int64_t hx = (int64_t)i * g.st[3][0] + (j * g.st[3][1] + k);       // Hx[i, j, k]
+    const int64_t hy = (int64_t)(i + 1) * g.st[4][0] + (j * g.st[4][1] + k); // Hy[i+1, j, k]
+    const int64_t hz = (int64_t)(i + 1) * g.st[5][0] + (j * g.st[5][1] + k); // Hz[i+1, j, k]
+    const R hz_a = ldf<P, 5>(g, hz + g.st[5][1]);             // Hz[i+1, j+1, k]
+    const R hz_b = ldf<P, 5>(g, hz);                          // Hz[i+1, j,   k]
+    const R hz_c = ldf<P, 5>(g, hz + g.st[5][1] - g.st[5][0]); // Hz[i,   j+1, k]
+    const R hy_a = ldf<P, 4>(g, hy + 1);                      // Hy[i+1, j, k+1]
+    const R hy_b = ldf<P, 4>(g, hy);                          // Hy[i+1, j, k]
+    const R hy_c = ldf<P, 4>(g, hy + 1 - g.st[4][0]);         // Hy[i,   j, k+1]
+    const R hx_a = ldf<P, 3>(g, hx + g.st[3][1] + 1);         // Hx[i, j+1, k+1]
+    const R hx_b = ldf<P, 3>(g, hx + g.st[3][1]);             // Hx[i, j+1, k]
+    const R hx_c = ldf<P, 3>(g, hx + 1);                      // Hx[i, j,   k+1]
+    const Pre<P> px = pre_of<P, 0, STRICT>(g, lx, idx);
+    const Pre<P> py = pre_of<P, 1, STRICT>(g, ly, idy);
+    const Pre<P> pz = pre_of<P, 2, STRICT>(g, lz, idz);
+    upd<P, 0, STRICT, DISP>(g, lx, i, j, k, hz_a - hz_b, hy_a - hy_b, ex, idx, px);
+    upd<P, 1, STRICT, DISP>(g, ly, i, j, k, hx_a - hx_b, hz_a - hz_c, ey, idy, py);
+    upd<P, 2, STRICT, DISP>(g, lz, i, j, k, hy_a - hy_c, hx_a - hx_c, ez, idz, pz);
   } else {
-    // H half.  Ez[i, j, k] and Ey[i, j, k] carried along i.
-    R ez_cur = ldc<P, 2>(g, (int64_t)ibeg * sz0 + j * sz1 + k);
-    R ey_cur = ldc<P, 1>(g, (int64_t)ibeg * sy0 + j * sy1 + k);
-    for (int i = ibeg; i < iend; ++i) {
-      const int64_t ezb = (int64_t)i * sz0 + j * sz1 + k;
-      const int64_t eyb = (int64_t)i * sy0 + j * sy1 + k;
-      const int64_t exb = (int64_t)i * sx0 + j * sx1 + k;
-      const R ez_n = ldc<P, 2>(g, ezb + sz0);      // Ez[i+1, j, k]
-      const R ez_j = ldc<P, 2>(g, ezb + sz1);      // Ez[i, j+1, k]
-      const R ey_n = ldc<P, 1>(g, eyb + sy0);      // Ey[i+1, j, k]
-      const R ey_k = ldc<P, 1>(g, eyb + 1);        // Ey[i, j, k+1]
-      const R ex_0 = ldc<P, 0>(g, exb);            // Ex[i, j, k]
-      const R ex_k = ldc<P, 0>(g, exb + 1);        // Ex[i, j, k+1]
-      const R ex_j = ldc<P, 0>(g, exb + sx1);      // Ex[i, j+1, k]
-      upd<P, 3, STRICT, DISP>(g, (int64_t)i * hx0 + (j + 1) * hx1 + k + 1, i, j + 1, k + 1,
-                              ez_j - ez_cur, ey_k - ey_cur);
-      upd<P, 4, STRICT, DISP>(g, (int64_t)(i + 1) * hy0 + j * hy1 + k + 1, i + 1, j, k + 1,
-                              ex_k - ex_0, ez_n - ez_cur);
-      upd<P, 5, STRICT, DISP>(g, (int64_t)(i + 1) * hz0 + (j + 1) * hz1 + k, i + 1, j + 1, k,
-                              ey_n - ey_cur, ex_j - ex_0);
-      ez_cur = ez_n;
-      ey_cur = ey_n;
-    }
+    // own points: Hx[i, j+1, k+1], Hy[i+1, j, k+1], Hz[i+1, j+1, k]
+    const int64_t lx = (int64_t)i * g.st[3][0] + ((j + 1) * g.st[3][1] + k + 1);
+    const int64_t ly = (int64_t)(i + 1) * g.st[4][0] + (j * g.st[4][1] + k + 1);
+    const int64_t lz = (int64_t)(i + 1) * g.st[5][0] + ((j + 1) * g.st[5][1] + k);
+    const uint8_t idx = ldc<3>(g, lx), idy = ldc<4>(g, ly), idz = ldc<5>(g, lz);
+    const R hx = ldf<P, 3>(g, lx), hy = ldf<P, 4>(g, ly), hz = ldf<P, 5>(g, lz);
+    const int64_t ex = (int64_t)i * g.st[0][0] + (j * g.st[0][1] + k);
+    const int64_t ey = (int64_t)i * g.st[1][0] + (j * g.st[1][1] + k);
+    const int64_t ez = (int64_t)i * g.st[2][0] + (j * g.st[2][1] + k);
+    const R ez_0 = ldf<P, 2>(g, ez);                 // Ez[i, j, k]
+    const R ez_j = ldf<P, 2>(g, ez + g.st[2][1]);    // Ez[i, j+1, k]
+    const R ez_i = ldf<P, 2>(g, ez + g.st[2][0]);    // Ez[i+1, j, k]
+    const R ey_0 = ldf<P, 1>(g, ey);                 // Ey[i, j, k]
+    const R ey_k = ldf<P, 1>(g, ey + 1);             // Ey[i, j, k+1]
+    const R ey_i = ldf<P, 1>(g, ey + g.st[1][0]);    // Ey[i+1, j, k]
+    const R ex_0 = ldf<P, 0>(g, ex);                 // Ex[i, j, k]
+    const R ex_k = ldf<P, 0>(g, ex + 1);             // Ex[i, j, k+1]
+    const R ex_j = ldf<P, 0>(g, ex + g.st[0][1]);    // Ex[i, j+1, k]
+    const Pre<P> px = pre_of<P, 3, STRICT>(g, lx, idx);
+    const Pre<P> py = pre_of<P, 4, STRICT>(g, ly, idy);
+    const Pre<P> pz = pre_of<P, 5, STRICT>(g, lz, idz);
+    upd<P, 3, STRICT, DISP>(g, lx, i, j + 1, k + 1, ez_j - ez_0, ey_k - ey_0, hx, idx, px);
+    upd<P, 4, STRICT, DISP>(g, ly, i + 1, j, k + 1, ex_k - ex_0, ez_i - ez_0, hy, idy, py);
+    upd<P, 5, STRICT, DISP>(g, lz, i + 1, j + 1, k, ey_i - ey_0, ex_j - ex_0, hz, idz, pz);
   }
 }
 
@@ -531,8 +496,6 @@ __global__ void k_sources(const GridDev g, int side, int64_t slot) {
 template <class P, bool STRICT>
 void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp) {
   using T = typename P::T;
-  const int64_t plane = (int64_t)d.n[1] * d.n[2];
-  const unsigned bx = (unsigned)((plane + kThreads - 1) / kThreads);
   int64_t maxplane = 1;
   for (int c = 0; c < 6; ++c)
     for (int a = 0; a < 3; ++a)
@@ -543,29 +506,19 @@ void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp) {
   const dim3 ggrid((unsigned)((maxplane + 255) / 256), 6);
   constexpr int kMaxY = 65535;
   k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
-  if (d.n[2] >= 32) {
-    const dim3 grid((unsigned)((d.n[2] + 31) / 32), (unsigned)((d.n[1] + 7) / 8),
-                    (unsigned)((d.n[0] + kIChunk - 1) / kIChunk));
-    const dim3 block(32, 8);
+  int bx_log2 = 0;
+  while (bx_log2 < 5 && (1 << bx_log2) < d.n[2]) ++bx_log2;
+  const int bx = 1 << bx_log2, by = kThreads / bx;
+  for (int i0 = 0; i0 < d.n[0]; i0 += kMaxY) {
+    const dim3 grid((unsigned)((d.n[2] + bx - 1) / bx), (unsigned)((d.n[1] + by - 1) / by),
+                    (unsigned)min(kMaxY, d.n[0] - i0));
     if (side == 0) {
       if (disp)
-        k_march<P, 0, STRICT, true><<<grid, block, 0, s>>>(d, kIChunk);
+        k_cell<P, 0, STRICT, true><<<grid, kThreads, 0, s>>>(d, bx_log2, i0);
       else
-        k_march<P, 0, STRICT, false><<<grid, block, 0, s>>>(d, kIChunk);
+        k_cell<P, 0, STRICT, false><<<grid, kThreads, 0, s>>>(d, bx_log2, i0);
     } else {
-      k_march<P, 1, STRICT, false><<<grid, block, 0, s>>>(d, kIChunk);
-    }
-  } else {
-    for (int i0 = 0; i0 < d.n[0]; i0 += kMaxY) {
-      const dim3 grid(bx, (unsigned)min(kMaxY, d.n[0] - i0));
-      if (side == 0) {
-        if (disp)
-          k_half<P, 0, STRICT, true><<<grid, kThreads, 0, s>>>(d, i0);
-        else
-          k_half<P, 0, STRICT, false><<<grid, kThreads, 0, s>>>(d, i0);
-      } else {
-        k_half<P, 1, STRICT, false><<<grid, kThreads, 0, s>>>(d, i0);
-      }
+      k_cell<P, 1, STRICT, false><<<grid, kThreads, 0, s>>>(d, bx_log2, i0);
     }
   }
   if (d.nsrc > 0)

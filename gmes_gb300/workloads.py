@@ -29,8 +29,12 @@ def air2d(precision="fp64", verbose=False):
     return TMzFDTD(space, geom, src, verbose=verbose, precision=precision), 286
 
 
-def cube(n=256, nobj=24, seed=0, pml_cells=10, precision="fp64", verbose=False, res=10):
-    """The 3-D dielectric + CPML benchmark scene on an n^3 grid (resolution 10)."""
+def cube(n=256, nobj=24, seed=0, pml_cells=10, precision="fp64", verbose=False, res=10,
+         src_time=None):
+    """The 3-D dielectric + CPML benchmark scene on an n^3 grid (resolution 10).
+
+    ``src_time`` replaces the Bandpass(0.5, 0.2) pulse (peak at t = 50).
+    """
     rng = np.random.default_rng(seed)
     dx = 1.0 / res
     size = n * dx
@@ -47,14 +51,14 @@ def cube(n=256, nobj=24, seed=0, pml_cells=10, precision="fp64", verbose=False, 
             geom.append(Block(material=Dielectric(eps_inf=eps), center=center,
                               size=(2 * r, 2 * r, 2 * r)))
     geom.append(Shell(material=Cpml(), thickness=pml_cells * dx))
-    src = [PointSource(src_time=Bandpass(freq=0.5, fwidth=0.2), center=(0, 0, 0),
+    src = [PointSource(src_time=src_time or Bandpass(freq=0.5, fwidth=0.2), center=(0, 0, 0),
                        component=Ex)]
     space = Cartesian(size=(size, size, size), resolution=res)
     return FDTD(space, geom, src, verbose=verbose, precision=precision), 1000
 
 
 def dispersive(n=192, seed=0, pml_cells=12, precision="fp64", verbose=False, res=20,
-               courant_ratio=0.6):
+               courant_ratio=0.6, src_time=None):
     """The 3-D dispersive + UPML benchmark scene on an n^3 grid (resolution 20).
 
     dt follows the background medium (eps = 2.25) as in the reference, so
@@ -85,7 +89,7 @@ def dispersive(n=192, seed=0, pml_cells=12, precision="fp64", verbose=False, res
                                        cps=cps),
                        center=(0.4 * inner, -0.4 * inner, 0.7 * inner), radius=0.2 * inner))
     geom.append(Shell(material=Upml(), thickness=pml_cells * dx))
-    src = [PointSource(src_time=Bandpass(freq=0.5, fwidth=0.2), center=(0, 0, 0),
+    src = [PointSource(src_time=src_time or Bandpass(freq=0.5, fwidth=0.2), center=(0, 0, 0),
                        component=Ez)]
     space = Cartesian(size=(size, size, size), resolution=res)
     return FDTD(space, geom, src, verbose=verbose, precision=precision,
