@@ -108,6 +108,7 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
     d.st[c][0] = sh[1] * sh[2];
     d.st[c][1] = sh[2];
     d.npts[c] = sh[0] * sh[1] * sh[2];
+    d.naux[c] = g.naux[c];
     d.f[c] = g.field[c];
     d.cls[c] = g.cls[c];
     d.aux[c] = g.aux[c];

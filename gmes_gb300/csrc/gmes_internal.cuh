@@ -23,6 +23,11 @@ struct Coef {
   float hi, lo;
 };
 
+// True unless the coefficient is +0 or -0 (bit test: no FP64 instruction).
+__device__ __forceinline__ bool coef_nonzero(const Coef* c) {
+  return (__ldg(reinterpret_cast<const unsigned long long*>(&c->d)) << 1) != 0ull;
+}
+
 __host__ __device__ inline Coef make_coef(double v) {
   Coef c;
   c.d = v;
@@ -130,6 +135,7 @@ struct GridDev {
   int64_t sh[6][3];       // component shapes
   int64_t st[6][2];       // strides of axes 0 and 1 (axis 2 stride is 1)
   int64_t npts[6];        // points per component
+  int32_t naux[6];        // state slots per point
   void* f[6];
   const uint8_t* cls[6];
   void* aux[6];
@@ -194,6 +200,7 @@ struct PolF64 {
   static __device__ __forceinline__ R ldw(const T* p) { return *p; }
   static __device__ __forceinline__ void st(T* p, R v) { *p = v; }
   static __device__ __forceinline__ R cf(const Coef& c) { return c.d; }
+  static __device__ __forceinline__ R cfg(const Coef* c) { return __ldg(&c->d); }
   static __device__ __forceinline__ R zero() { return 0.0; }
   static __device__ __forceinline__ R from_double(double v) { return v; }
 };
@@ -205,6 +212,7 @@ struct PolF32 {
   static __device__ __forceinline__ R ldw(const T* p) { return *p; }
   static __device__ __forceinline__ void st(T* p, R v) { *p = v; }
   static __device__ __forceinline__ R cf(const Coef& c) { return c.hi; }
+  static __device__ __forceinline__ R cfg(const Coef* c) { return __ldg(&c->hi); }
   static __device__ __forceinline__ R zero() { return 0.f; }
   static __device__ __forceinline__ R from_double(double v) { return static_cast<float>(v); }
 };
@@ -222,6 +230,10 @@ struct PolDF {
   }
   static __device__ __forceinline__ void st(T* p, R v) { *p = make_float2(v.hi, v.lo); }
   static __device__ __forceinline__ R cf(const Coef& c) { return {c.hi, c.lo}; }
+  static __device__ __forceinline__ R cfg(const Coef* c) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(&c->hi));
+    return {v.x, v.y};
+  }
   static __device__ __forceinline__ R zero() { return {0.f, 0.f}; }
   static __device__ __forceinline__ R from_double(double v) {
     const float h = static_cast<float>(v);
