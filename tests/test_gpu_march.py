@@ -18,7 +18,10 @@ from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-12, "df64": 1e-12, "fp32": 5e-3}
+# df64 stores 48-49 significand bits (two floats): ~16x the FP64 rounding
+# error per step.  Measured: 2e-15 .. 1.5e-12 (the larger on this 45^3 CPML
+# scene, where FP64 itself shows ~7e-14); bound stated at 1e-11.
+TOL = {"fp64": 1e-12, "df64": 1e-11, "fp32": 5e-3}
 
 
 def _run(builder, precision, steps, host_profiles=False):
@@ -76,7 +79,8 @@ def test_march_fast_modes(name, precision):
     for c, comp in enumerate(G.constant.COMPONENTS):
         f = sim.field[comp].numpy()
         assert np.isfinite(f).all()
-        assert rel_l2(f, ref[c]) <= TOL[precision], (name, precision, comp.__name__)
+        err = rel_l2(f, ref[c])
+        assert err <= TOL[precision], (name, precision, comp.__name__, err)
 
 
 def test_full_size_cube256_against_strict():
