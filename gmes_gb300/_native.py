@@ -24,6 +24,9 @@ EXPORTS = [
     "gmes_grid_sizes", "gmes_build_coefficients", "gmes_set_pml_profile",
     "gmes_get_pml_profile", "gmes_reset",
     "gmes_step", "gmes_half_step", "gmes_read_field", "gmes_write_field",
+    "gmes_batch_workspace_size", "gmes_batch_prepare", "gmes_batch_set_steps", "gmes_batch_step",
+    "gmes_graph_capture_step", "gmes_graph_capture_batch", "gmes_graph_launch",
+    "gmes_graph_destroy",
 ]
 
 
@@ -54,6 +57,12 @@ class GridDescC(C.Structure):
         ("field", C.c_void_p * 6), ("cls", C.c_void_p * 6), ("aux", C.c_void_p * 6),
         ("coef", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p),
     ]
+
+
+class BatchC(C.Structure):
+    _fields_ = [("njobs", C.c_int32), ("precision", C.c_int32), ("dispersive", C.c_int32),
+                ("srcs", C.c_int32), ("tiles", C.c_int64), ("ghosts", C.c_int64),
+                ("workspace", C.c_void_p), ("workspace_bytes", C.c_int64)]
 
 
 class GmesError(RuntimeError):
@@ -92,8 +101,21 @@ def load():
     lib.gmes_half_step.argtypes = [P(GridDescC), C.c_int32, C.c_int32, C.c_void_p]
     lib.gmes_read_field.argtypes = [P(GridDescC), C.c_int32, P(C.c_double), C.c_void_p]
     lib.gmes_write_field.argtypes = [P(GridDescC), C.c_int32, P(C.c_double), C.c_void_p]
+    lib.gmes_batch_workspace_size.restype = C.c_int64
+    lib.gmes_batch_workspace_size.argtypes = [C.c_int32]
+    lib.gmes_batch_prepare.argtypes = [P(P(GridDescC)), C.c_int32, C.c_void_p, C.c_int64,
+                                       C.c_int32, P(BatchC), C.c_void_p]
+    lib.gmes_batch_set_steps.argtypes = [P(BatchC), P(C.c_int32), C.c_void_p]
+    lib.gmes_batch_step.argtypes = [P(BatchC), C.c_int32, C.c_int32, C.c_void_p]
+    lib.gmes_graph_capture_step.argtypes = [P(GridDescC), C.c_int32, C.c_void_p,
+                                            P(C.c_void_p)]
+    lib.gmes_graph_capture_batch.argtypes = [P(BatchC), C.c_int32, C.c_int32, C.c_void_p,
+                                             P(C.c_void_p)]
+    lib.gmes_graph_launch.argtypes = [C.c_void_p, C.c_void_p]
+    lib.gmes_graph_destroy.argtypes = [C.c_void_p]
     for name in EXPORTS:
-        if name not in ("gmes_abi_version", "gmes_last_error", "gmes_elem_size"):
+        if name not in ("gmes_abi_version", "gmes_last_error", "gmes_elem_size",
+                        "gmes_batch_workspace_size"):
             getattr(lib, name).restype = C.c_int
     if lib.gmes_abi_version() != ABI_VERSION:
         raise RuntimeError(f"{LIB_PATH}: ABI {lib.gmes_abi_version()}, expected {ABI_VERSION}")

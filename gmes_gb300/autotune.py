@@ -1,0 +1,80 @@
+"""Launch-shape autotuner for the multi-grid (batch) kernels.
+
+The batch update kernel has two shape knobs: the block's extent along k
+(``bx_cap``: 2**bx_cap threads along k, the rest along j) and the grid size
+of the persistent kernel (``blocks``; 0 = one block per tile).  Which is
+best depends on the mix of grid shapes (thin 2-D grids want short k extents,
+large 3-D grids want full warps along k and enough blocks to hide memory
+latency).  The tuner measures candidates on live chunks -- every candidate
+computes exactly the same values, so tuning costs no extra work -- and
+keeps the fastest per mix bucket.
+"""
+
+import time
+
+
+def _sms():
+    from .engine import _torch
+    torch = _torch()
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
+class Tuner:
+    """Per-bucket choice of (bx_cap, blocks) from measured chunk throughput."""
+
+    def __init__(self, candidates=None, trials_per_candidate=1):
+        sms = _sms()
+        self.candidates = candidates or [
+            (5, 0), (4, 0), (3, 0), (5, 8 * sms), (5, 32 * sms), (4, 16 * sms)]
+        self.trials_per_candidate = int(trials_per_candidate)
+        self.best = {}
+        self.results = {}
+        self._key = None
+        self._cand = None
+        self._t0 = None
+
+    @staticmethod
+    def bucket(jobs):
+        """Mix bucket: number of grids (power of 2), dimensionality, size scale."""
+        n = len(jobs)
+        nb = 1
+        while nb < n:
+            nb *= 2
+        thin = sum(1 for j in jobs if j.scene.n[2] < 32)
+        cells = sorted(j.scene.cells for j in jobs)
+        med = cells[len(cells) // 2]
+        scale = 0
+        while (1 << (2 * scale + 10)) < med:
+            scale += 1
+        return (nb, "2d" if thin * 2 > n else "3d", scale)
+
+    def choice(self, jobs):
+        key = self.bucket(jobs)
+        self._key = key
+        if key in self.best:
+            self._cand = self.best[key]
+            return self._cand
+        tried = self.results.setdefault(key, {})
+        for cand in self.candidates:
+            if len(tried.get(cand, [])) < self.trials_per_candidate:
+                self._cand = cand
+                return cand
+        self.best[key] = max(tried, key=lambda c: max(tried[c]))
+        self._cand = self.best[key]
+        return self._cand
+
+    def observe_start(self, batch):
+        self._t0 = time.perf_counter()
+
+    def observe_end(self, batch, cell_updates):
+        if self._t0 is None or self._key is None or self._key in self.best:
+            return
+        dt = time.perf_counter() - self._t0
+        cand = (batch.bx_cap, batch.blocks)
+        if dt > 0:
+            self.results.setdefault(self._key, {}).setdefault(cand, []).append(cell_updates / dt)
+
+    def summary(self):
+        return {str(k): {"best": v, "measured": {str(c): max(r) for c, r in
+                                                  self.results.get(k, {}).items()}}
+                for k, v in self.best.items()}

@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -121,6 +122,54 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
   d.src = g.src;
   d.src_val = g.src_val;
   return d;
+}
+
+struct BatchLayout {
+  int64_t jobs, tile_prefix, bxl, steps, ghost_prefix, src_prefix, total;
+};
+
+BatchLayout batch_layout(int32_t njobs) {
+  BatchLayout L;
+  int64_t off = 0;
+  L.jobs = off;
+  off = align256(off + (int64_t)njobs * (int64_t)sizeof(GridDev));
+  L.tile_prefix = off;
+  off = align256(off + (int64_t)(njobs + 1) * 8);
+  L.bxl = off;
+  off = align256(off + (int64_t)njobs * 4);
+  L.steps = off;
+  off = align256(off + (int64_t)njobs * 4);
+  L.ghost_prefix = off;
+  off = align256(off + (int64_t)(njobs + 1) * 8);
+  L.src_prefix = off;
+  off = align256(off + (int64_t)(njobs + 1) * 4);
+  L.total = off;
+  return L;
+}
+
+BatchView batch_view(const gmes_batch& b) {
+  const BatchLayout L = batch_layout(b.njobs);
+  char* w = static_cast<char*>(b.workspace);
+  BatchView v;
+  v.jobs = reinterpret_cast<const GridDev*>(w + L.jobs);
+  v.tile_prefix = reinterpret_cast<const int64_t*>(w + L.tile_prefix);
+  v.bxl = reinterpret_cast<const int32_t*>(w + L.bxl);
+  v.steps = reinterpret_cast<const int32_t*>(w + L.steps);
+  v.ghost_prefix = reinterpret_cast<const int64_t*>(w + L.ghost_prefix);
+  v.src_prefix = reinterpret_cast<const int32_t*>(w + L.src_prefix);
+  v.njobs = b.njobs;
+  v.srcs = b.srcs;
+  v.tiles = b.tiles;
+  v.ghosts = b.ghosts;
+  return v;
+}
+
+int64_t max_ghost_plane(const GridDev& d) {
+  int64_t m = 1;
+  for (int c = 0; c < 6; ++c)
+    for (int a = 0; a < 3; ++a)
+      for (int b = a + 1; b < 3; ++b) m = d.sh[c][a] * d.sh[c][b] > m ? d.sh[c][a] * d.sh[c][b] : m;
+  return m;
 }
 
 }  // namespace gmes
@@ -353,6 +402,142 @@ gmes_status gmes_half_step(const gmes_grid_desc* g, int32_t side, int32_t step, 
   const GridDev d = make_grid_dev(*g);
   cudaError_t e = launch_half(*g, d, side, step, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching half-step kernels");
+  return GMES_OK;
+}
+
+int64_t gmes_batch_workspace_size(int32_t njobs) {
+  if (njobs < 1) return 0;
+  return batch_layout(njobs).total;
+}
+
+gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs,
+                               void* workspace, int64_t workspace_bytes, int32_t bx_cap,
+                               gmes_batch* out, void* stream) {
+  if (grids == nullptr || out == nullptr || workspace == nullptr)
+    return fail(GMES_ERR_VALUE, "NULL argument");
+  if (njobs < 1) return fail(GMES_ERR_VALUE, "njobs = %d must be >= 1", njobs);
+  if (bx_cap < 0 || bx_cap > 5) return fail(GMES_ERR_VALUE, "bx_cap = %d outside [0, 5]", bx_cap);
+  if (bx_cap == 0) bx_cap = 5;
+  const BatchLayout L = batch_layout(njobs);
+  if (workspace_bytes < L.total)
+    return fail(GMES_ERR_VALUE, "workspace of %lld bytes, %lld needed",
+                (long long)workspace_bytes, (long long)L.total);
+  std::vector<char> host(L.total, 0);
+  GridDev* jobs = reinterpret_cast<GridDev*>(host.data() + L.jobs);
+  int64_t* tp = reinterpret_cast<int64_t*>(host.data() + L.tile_prefix);
+  int32_t* bxl = reinterpret_cast<int32_t*>(host.data() + L.bxl);
+  int32_t* steps = reinterpret_cast<int32_t*>(host.data() + L.steps);
+  int64_t* gp = reinterpret_cast<int64_t*>(host.data() + L.ghost_prefix);
+  int32_t* sp = reinterpret_cast<int32_t*>(host.data() + L.src_prefix);
+  int32_t precision = -1;
+  bool disp = false;
+  tp[0] = 0;
+  gp[0] = 0;
+  sp[0] = 0;
+  for (int q = 0; q < njobs; ++q) {
+    const gmes_grid_desc* g = grids[q];
+    gmes_status st = check_desc(g, true);
+    if (st != GMES_OK) return fail(st, "grid %d: %s", q, g_last_error.c_str());
+    if (precision < 0) precision = g->precision;
+    if (g->precision != precision)
+      return fail(GMES_ERR_VALUE, "grid %d: all grids of a batch must share one precision", q);
+    disp = disp || (g->flags & GMES_FLAG_DISPERSIVE);
+    jobs[q] = make_grid_dev(*g);
+    int l = 0;
+    while (l < bx_cap && (1 << l) < g->n[2]) ++l;
+    bxl[q] = l;
+    const int64_t bx = 1 << l, by = kBatchThreads / bx;
+    const int64_t tiles = ((g->n[2] + bx - 1) / bx) * ((g->n[1] + by - 1) / by) * g->n[0];
+    tp[q + 1] = tp[q] + tiles;
+    gp[q + 1] = gp[q] + 6 * max_ghost_plane(jobs[q]);
+    sp[q + 1] = sp[q] + g->nsrc;
+    steps[q] = 0;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(workspace, host.data(), L.total, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "uploading the batch workspace");
+  out->njobs = njobs;
+  out->precision = precision;
+  out->dispersive = disp ? 1 : 0;
+  out->srcs = sp[njobs];
+  out->tiles = tp[njobs];
+  out->ghosts = gp[njobs];
+  out->workspace = workspace;
+  out->workspace_bytes = workspace_bytes;
+  return GMES_OK;
+}
+
+gmes_status gmes_batch_set_steps(const gmes_batch* b, const int32_t* steps, void* stream) {
+  if (b == nullptr || steps == nullptr || b->workspace == nullptr)
+    return fail(GMES_ERR_VALUE, "NULL argument");
+  for (int q = 0; q < b->njobs; ++q)
+    if (steps[q] < 0) return fail(GMES_ERR_VALUE, "steps[%d] = %d < 0", q, steps[q]);
+  const BatchLayout L = batch_layout(b->njobs);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(static_cast<char*>(b->workspace) + L.steps, steps,
+                                  b->njobs * sizeof(int32_t), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "uploading batch steps");
+  return GMES_OK;
+}
+
+gmes_status gmes_batch_step(const gmes_batch* b, int32_t nsteps, int32_t blocks, void* stream) {
+  if (b == nullptr || b->workspace == nullptr) return fail(GMES_ERR_VALUE, "NULL argument");
+  if (nsteps < 0 || blocks < 0) return fail(GMES_ERR_VALUE, "negative nsteps or blocks");
+  if (b->njobs < 1) return fail(GMES_ERR_VALUE, "empty batch");
+  if (nsteps == 0) return GMES_OK;
+  cudaError_t e = launch_batch(batch_view(*b), b->precision, b->dispersive != 0, nsteps, blocks,
+                               static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching batch kernels");
+  return GMES_OK;
+}
+
+static gmes_status capture(cudaStream_t s, void** exec_out,
+                           const std::function<gmes_status()>& body) {
+  if (s == nullptr) return fail(GMES_ERR_VALUE, "graph capture needs a non-default stream");
+  if (exec_out == nullptr) return fail(GMES_ERR_VALUE, "graph_exec is NULL");
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(e, "beginning stream capture");
+  gmes_status st = body();
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(s, &graph);
+  if (st != GMES_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "ending stream capture");
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e, "instantiating graph");
+  *exec_out = exec;
+  return GMES_OK;
+}
+
+gmes_status gmes_graph_capture_step(const gmes_grid_desc* g, int32_t nsteps, void* stream,
+                                    void** graph_exec) {
+  return capture(static_cast<cudaStream_t>(stream), graph_exec,
+                 [&]() { return gmes_step(g, nsteps, stream); });
+}
+
+gmes_status gmes_graph_capture_batch(const gmes_batch* b, int32_t nsteps, int32_t blocks,
+                                     void* stream, void** graph_exec) {
+  return capture(static_cast<cudaStream_t>(stream), graph_exec,
+                 [&]() { return gmes_batch_step(b, nsteps, blocks, stream); });
+}
+
+gmes_status gmes_graph_launch(void* graph_exec, void* stream) {
+  if (graph_exec == nullptr) return fail(GMES_ERR_VALUE, "graph_exec is NULL");
+  cudaError_t e = cudaGraphLaunch(static_cast<cudaGraphExec_t>(graph_exec),
+                                  static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching graph");
+  return GMES_OK;
+}
+
+gmes_status gmes_graph_destroy(void* graph_exec) {
+  if (graph_exec == nullptr) return GMES_OK;
+  cudaError_t e = cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(graph_exec));
+  if (e != cudaSuccess) return cuda_fail(e, "destroying graph");
   return GMES_OK;
 }
 

@@ -241,6 +241,23 @@ struct PolDF {
   }
 };
 
+// Threads per block of the half-step kernels (single grid and batch).
+constexpr int kBatchThreads = 256;
+
+// Kernel-side view of a batch workspace (gmes_batch_prepare).
+struct BatchView {
+  const GridDev* jobs;
+  const int64_t* tile_prefix;   // [njobs + 1] blocks of each grid's half-step
+  const int32_t* bxl;           // per grid: log2 of the block's k extent
+  const int32_t* steps;         // per grid: steps to take in this chunk
+  const int64_t* ghost_prefix;  // [njobs + 1] 6 x (largest ghost plane) per grid
+  const int32_t* src_prefix;    // [njobs + 1] point sources
+  int32_t njobs;
+  int32_t srcs;
+  int64_t tiles;
+  int64_t ghosts;
+};
+
 // Host-side helpers implemented in gmes_capi.cu.
 GridDev make_grid_dev(const gmes_grid_desc& g);
 
@@ -249,6 +266,8 @@ cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps,
                         cudaStream_t s);
 cudaError_t launch_half(const gmes_grid_desc& g, const GridDev& d, int side, int step,
                         cudaStream_t s);
+cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nsteps, int blocks,
+                         cudaStream_t s);
 cudaError_t launch_build_coefficients(const gmes_grid_desc& g, const GridDev& d,
                                       cudaStream_t s);
 

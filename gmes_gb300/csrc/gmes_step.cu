@@ -385,16 +385,8 @@ __device__ __forceinline__ Pre<P> pre_of(const GridDev& g, int64_t lin, const in
 // MASK: the active-component mask when known at compile time, 0 when read
 // from the grid; I: offset type.  (Only <0, int64_t> is instantiated.)
 template <class P, int SIDE, bool STRICT, bool DISP, int MASK, class I>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
-    k_cell(const GridDev g, int bx_log2, int i0) {
+__device__ __forceinline__ void cell_body(const GridDev& g, int i, int j, int k) {
   using R = typename P::R;
-  const int bx = 1 << bx_log2;
-  const int tx = threadIdx.x & (bx - 1);
-  const int ty = threadIdx.x >> bx_log2;
-  const int k = blockIdx.x * bx + tx;
-  const int j = blockIdx.y * (kThreads >> bx_log2) + ty;
-  const int i = i0 + (int)blockIdx.z;
-  if (k >= g.n[2] || j >= g.n[1] || i >= g.n[0]) return;
   const I s00 = (I)g.st[0][0], s01 = (I)g.st[0][1], s10 = (I)g.st[1][0], s11 = (I)g.st[1][1];
   const I s20 = (I)g.st[2][0], s21 = (I)g.st[2][1], s30 = (I)g.st[3][0], s31 = (I)g.st[3][1];
   const I s40 = (I)g.st[4][0], s41 = (I)g.st[4][1], s50 = (I)g.st[5][0], s51 = (I)g.st[5][1];
@@ -455,6 +447,19 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
   }
 }
 
+template <class P, int SIDE, bool STRICT, bool DISP, int MASK, class I>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    k_cell(const GridDev g, int bx_log2, int i0) {
+  const int bx = 1 << bx_log2;
+  const int tx = threadIdx.x & (bx - 1);
+  const int ty = threadIdx.x >> bx_log2;
+  const int k = blockIdx.x * bx + tx;
+  const int j = blockIdx.y * (kThreads >> bx_log2) + ty;
+  const int i = i0 + (int)blockIdx.z;
+  if (k >= g.n[2] || j >= g.n[1] || i >= g.n[0]) return;
+  cell_body<P, SIDE, STRICT, DISP, MASK, I>(g, i, j, k);
+}
+
 template <class P, bool STRICT, int MASK, class I>
 void launch_cell(const GridDev& d, int side, bool disp, dim3 grid, int bx_log2, int i0,
                  cudaStream_t s) {
@@ -475,17 +480,15 @@ void launch_cell(const GridDev& d, int side, bool disp, dim3 grid, int bx_log2, 
 // ghost coordinate at once, so corners get the value the reference's two
 // successive plane copies give them and no source is itself a ghost.
 template <class T>
-__global__ void k_ghost(const GridDev g, int side, int64_t maxplane) {
-  const int item = blockIdx.y;  // component-in-side * 2 + which ghost axis
+__device__ __forceinline__ void ghost_point(const GridDev& g, int side, int item, int64_t t) {
   const int c = side * 3 + item / 2;
   if (!(g.active & (1 << c))) return;
   const int own = c % 3;
   const int ga = (item & 1) ? (own + 2) % 3 : (own + 1) % 3;
   const int pa = (ga + 1) % 3, qa = (ga + 2) % 3;
   const int p_ = pa < qa ? pa : qa, q_ = pa < qa ? qa : pa;  // q_ is the faster axis
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t np = g.sh[c][p_] * g.sh[c][q_];
-  if (t >= np || t >= maxplane) return;
+  if (t >= np) return;
   int64_t x[3];
   x[p_] = t / g.sh[c][q_];
   x[q_] = t - x[p_] * g.sh[c][q_];
@@ -506,12 +509,17 @@ __global__ void k_ghost(const GridDev g, int side, int64_t maxplane) {
   f[dst] = f[src];
 }
 
+template <class T>
+__global__ void k_ghost(const GridDev g, int side, int64_t maxplane) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= maxplane) return;
+  ghost_point<T>(g, side, blockIdx.y, t);
+}
+
 // Point sources of one half-step (gmes/pw_source.py:74-131), applied after
 // that half's material update.  `v` has been computed on the host in FP64.
 template <class P, bool STRICT>
-__global__ void k_sources(const GridDev g, int side, int64_t slot) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= g.nsrc) return;
+__device__ __forceinline__ void source_point(const GridDev& g, int side, int64_t slot, int q) {
   const gmes_point_source ps = g.src[q];
   // the table is caller-provided device memory: skip entries that do not
   // name a point of an active component
@@ -527,6 +535,77 @@ __global__ void k_sources(const GridDev g, int side, int64_t slot) {
     *reinterpret_cast<double*>(f) = __dsub_rn(*reinterpret_cast<double*>(f), v);
   } else {
     P::st(f, P::ldw(f) - P::from_double(v));
+  }
+}
+
+// Point sources of one half-step (gmes/pw_source.py:74-131), applied after
+// that half's material update.  The values were computed on the host in FP64.
+template <class P, bool STRICT>
+__global__ void k_sources(const GridDev g, int side, int64_t slot) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= g.nsrc) return;
+  source_point<P, STRICT>(g, side, slot, q);
+}
+
+// ---------------------------------------------------------------------------
+// Multi-grid ("batch") form: one launch per half-step advances every grid of
+// a batch.  The per-grid views live in a caller-allocated workspace with
+// prefix sums of each grid's blocks, ghost-plane points and sources; a block
+// (or thread) finds its grid by binary search in the prefix array and runs
+// exactly the per-grid code, so a grid's result does not depend on what else
+// is in the batch.  Grids with steps[g] <= s sit out step s of the chunk.
+// ---------------------------------------------------------------------------
+template <class I>
+__device__ __forceinline__ int find_job(const I* prefix, int njobs, I v) {
+  int lo = 0, hi = njobs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(prefix + mid) <= v)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+template <class P, int SIDE, bool STRICT, bool DISP>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_multi_cell(const BatchView v, int s) {
+  for (int64_t b = blockIdx.x; b < v.tiles; b += gridDim.x) {
+    const int job = find_job<int64_t>(v.tile_prefix, v.njobs, b);
+    if (s >= __ldg(v.steps + job)) continue;
+    const GridDev& g = v.jobs[job];
+    const int bxl = __ldg(v.bxl + job);
+    const int bx = 1 << bxl, by = kThreads >> bxl;
+    const int nkb = (g.n[2] + bx - 1) / bx, njb = (g.n[1] + by - 1) / by;
+    const int64_t local = b - __ldg(v.tile_prefix + job);
+    const int i = (int)(local / ((int64_t)nkb * njb));
+    const int rem = (int)(local - (int64_t)i * nkb * njb);
+    const int jb = rem / nkb, kb = rem - jb * nkb;
+    const int k = kb * bx + (threadIdx.x & (bx - 1));
+    const int j = jb * by + (threadIdx.x >> bxl);
+    if (k < g.n[2] && j < g.n[1]) cell_body<P, SIDE, STRICT, DISP, 0, int64_t>(g, i, j, k);
+  }
+}
+
+template <class T>
+__global__ void k_multi_ghost(const BatchView v, int side, int s) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < v.ghosts;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int job = find_job<int64_t>(v.ghost_prefix, v.njobs, t);
+    if (s >= __ldg(v.steps + job)) continue;
+    const GridDev& g = v.jobs[job];
+    const int64_t local = t - __ldg(v.ghost_prefix + job);
+    const int64_t per = (__ldg(v.ghost_prefix + job + 1) - __ldg(v.ghost_prefix + job)) / 6;
+    ghost_point<T>(g, side, (int)(local / per), local % per);
+  }
+}
+
+template <class P, bool STRICT>
+__global__ void k_multi_sources(const BatchView v, int side, int s) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < v.srcs; t += gridDim.x * blockDim.x) {
+    const int job = find_job<int>(v.src_prefix, v.njobs, t);
+    if (s >= __ldg(v.steps + job)) continue;
+    source_point<P, STRICT>(v.jobs[job], side, 2 * (int64_t)s + side, t - __ldg(v.src_prefix + job));
   }
 }
 
@@ -595,6 +674,47 @@ cudaError_t dispatch_precision(const gmes_grid_desc& g, const GridDev& d, int ns
 }
 
 }  // namespace
+
+template <class P, bool STRICT>
+cudaError_t run_batch(const BatchView& v, bool disp, int nsteps, int blocks, cudaStream_t st) {
+  using T = typename P::T;
+  const int cells = blocks > 0 ? blocks : (int)(v.tiles < (1 << 30) ? v.tiles : (1 << 30));
+  const int gblocks = (int)((v.ghosts + 255) / 256 < 65535 * 16 ? (v.ghosts + 255) / 256 : 65535 * 16);
+  const int sblocks = (v.srcs + 127) / 128;
+  for (int s = 0; s < nsteps; ++s) {
+    for (int side = 0; side < 2; ++side) {
+      if (gblocks > 0) k_multi_ghost<T><<<gblocks, 256, 0, st>>>(v, 1 - side, s);
+      if (cells > 0) {
+        if (side == 0) {
+          if (disp)
+            k_multi_cell<P, 0, STRICT, true><<<cells, kThreads, 0, st>>>(v, s);
+          else
+            k_multi_cell<P, 0, STRICT, false><<<cells, kThreads, 0, st>>>(v, s);
+        } else {
+          k_multi_cell<P, 1, STRICT, false><<<cells, kThreads, 0, st>>>(v, s);
+        }
+      }
+      if (sblocks > 0) k_multi_sources<P, STRICT><<<sblocks, 128, 0, st>>>(v, side, s);
+    }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nsteps, int blocks,
+                         cudaStream_t s) {
+  switch (precision) {
+    case GMES_FP64:
+      return run_batch<PolF64, false>(v, disp, nsteps, blocks, s);
+    case GMES_FP64_STRICT:
+      return run_batch<PolF64, true>(v, disp, nsteps, blocks, s);
+    case GMES_FP32:
+      return run_batch<PolF32, false>(v, disp, nsteps, blocks, s);
+    case GMES_DF64:
+      return run_batch<PolDF, false>(v, disp, nsteps, blocks, s);
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
 
 cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps, cudaStream_t s) {
   return dispatch_precision(g, d, nsteps, 3, 0, s);

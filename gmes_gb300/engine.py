@@ -36,10 +36,12 @@ class GridEngine:
     ``src_chunk``: steps of source values staged per ``gmes_step`` call.
     """
 
-    def __init__(self, scene, precision="fp64", device=None, src_chunk=256):
+    def __init__(self, scene, precision="fp64", device=None, src_chunk=256, use_graphs=True):
         require_cuda()
         torch = _torch()
         self.lib = N.load()
+        self.use_graphs = bool(use_graphs)
+        self._graphs = {}
         self.scene = scene
         self.precision = precision
         self.prec = N.PRECISIONS[precision]
@@ -110,13 +112,44 @@ class GridEngine:
         self.desc = d
         self._staged = None
         self._rows, self._pool, self._pmls = rows, pool, pmls
+        # The engine works on its own (non-default) stream so that chunks of
+        # steps can be captured as CUDA graphs; it orders itself against the
+        # caller's current stream on entry and exit of every call.
+        self._stream = torch.cuda.Stream(device=dev)
+        self._enter()
         self.build_coefficients()
+        self._leave()
 
-    # -- setup -------------------------------------------------------------
+    def __del__(self):
+        graphs = getattr(self, "_graphs", {})
+        for h in graphs.values():
+            try:
+                self.lib.gmes_graph_destroy(h)
+            except Exception:
+                pass
+        graphs.clear()
+
+    # -- streams -----------------------------------------------------------
     @property
     def stream(self):
-        return _torch().cuda.current_stream(self.device).cuda_stream
+        """The engine's CUDA stream handle (cudaStream_t as an int)."""
+        return self._stream.cuda_stream
 
+    @property
+    def torch_stream(self):
+        return self._stream
+
+    def _enter(self):
+        cur = _torch().cuda.current_stream(self.device)
+        if cur.cuda_stream != self._stream.cuda_stream:
+            self._stream.wait_stream(cur)
+
+    def _leave(self):
+        cur = _torch().cuda.current_stream(self.device)
+        if cur.cuda_stream != self._stream.cuda_stream:
+            cur.wait_stream(self._stream)
+
+    # -- setup -------------------------------------------------------------
     def build_coefficients(self):
         rows, pool, pmls = self._rows, self._pool, self._pmls
         crow = (N.ClassDescC * max(1, len(rows)))()
@@ -138,6 +171,7 @@ class GridEngine:
                                                  C.c_void_p(self.stream)))
 
     def set_pml_profile(self, pml, comp, axis, values):
+        self._enter()
         v = np.ascontiguousarray(values, dtype=np.float64)
         N.check(self.lib.gmes_set_pml_profile(
             C.byref(self.desc), pml, comp, axis,
@@ -153,32 +187,59 @@ class GridEngine:
         return out
 
     def reset(self):
+        self._enter()
         N.check(self.lib.gmes_reset(C.byref(self.desc), C.c_void_p(self.stream)))
+        self._leave()
 
     # -- stepping ----------------------------------------------------------
+    def _graph(self, nsteps):
+        h = self._graphs.get(nsteps)
+        if h is None:
+            out = C.c_void_p()
+            N.check(self.lib.gmes_graph_capture_step(C.byref(self.desc), int(nsteps),
+                                                     C.c_void_p(self.stream), C.byref(out)))
+            h = self._graphs[nsteps] = out.value
+        return h
+
+    def _launch(self, nsteps):
+        if self.use_graphs:
+            N.check(self.lib.gmes_graph_launch(C.c_void_p(self._graph(nsteps)),
+                                               C.c_void_p(self.stream)))
+        else:
+            N.check(self.lib.gmes_step(C.byref(self.desc), int(nsteps), C.c_void_p(self.stream)))
+
+    def _stage(self, vals, k):
+        torch = _torch()
+        # the pinned staging buffer may still be read by the previous
+        # chunk's asynchronous copy
+        if self._staged is not None:
+            self._staged.synchronize()
+        self.src_host[:k].copy_(torch.from_numpy(np.ascontiguousarray(vals)))
+        with torch.cuda.stream(self._stream):
+            self.src_val[:k].copy_(self.src_host[:k], non_blocking=True)
+            self._staged = torch.cuda.Event()
+            self._staged.record(self._stream)
+
     def step(self, nsteps, n0=0.0, src_values=None):
         """Advance ``nsteps`` steps; the first E half-step is at n0 + 1/2.
 
-        ``src_values`` (nsteps, 2, nsrc) overrides the host evaluation of the
-        source-time functions.
+        Steps run in chunks of up to ``src_chunk``: the source values of a
+        chunk are staged, then the chunk runs as one CUDA graph (or as plain
+        launches with ``use_graphs=False``).  ``src_values`` (nsteps, 2, nsrc)
+        overrides the host evaluation of the source-time functions.
         """
         nsteps = int(nsteps)
+        self._enter()
         done = 0
         while done < nsteps:
             k = min(self.src_chunk, nsteps - done)
             if self.src is not None:
                 vals = (src_values[done:done + k] if src_values is not None else
                         source_values(self.scene, self.scene.dt, n0 + done, k))
-                # the pinned staging buffer may still be read by the previous
-                # chunk's asynchronous copy
-                if self._staged is not None:
-                    self._staged.synchronize()
-                self.src_host[:k].copy_(_torch().from_numpy(np.ascontiguousarray(vals)))
-                self.src_val[:k].copy_(self.src_host[:k], non_blocking=True)
-                self._staged = _torch().cuda.Event()
-                self._staged.record()
-            N.check(self.lib.gmes_step(C.byref(self.desc), k, C.c_void_p(self.stream)))
+                self._stage(vals, k)
+            self._launch(k)
             done += k
+        self._leave()
 
     def half_step(self, side, slot=0):
         """Enqueue one half-step (0: E, 1: H) reading staged source slot ``slot``."""
@@ -191,17 +252,12 @@ class GridEngine:
             return
         if nsteps > self.src_chunk:
             raise ValueError("more steps than the staging buffer holds")
-        vals = source_values(self.scene, self.scene.dt, n0, nsteps)
-        if self._staged is not None:
-            self._staged.synchronize()
-        self.src_host[:nsteps].copy_(_torch().from_numpy(vals))
-        self.src_val[:nsteps].copy_(self.src_host[:nsteps], non_blocking=True)
-        self._staged = _torch().cuda.Event()
-        self._staged.record()
+        self._enter()
+        self._stage(source_values(self.scene, self.scene.dt, n0, nsteps), nsteps)
 
     def launch_raw(self, nsteps):
         """Enqueue ``nsteps`` steps with the source values already staged."""
-        N.check(self.lib.gmes_step(C.byref(self.desc), int(nsteps), C.c_void_p(self.stream)))
+        self._launch(int(nsteps))
 
     # -- field access ------------------------------------------------------
     def tensor(self, c):
@@ -260,4 +316,4 @@ class GridEngine:
         return a.view(torch.float32).view((na,) + shape + (2,))
 
     def synchronize(self):
-        _torch().cuda.synchronize(self.device)
+        self._stream.synchronize()

@@ -1,0 +1,263 @@
+"""Continuous-batching server for FDTD jobs.
+
+Jobs (a scene plus a step count) arrive over time.  The server keeps a
+resident set of grids on the GPU and advances all of them together in
+chunks of steps (``Batch``: one launch per kernel kind per half-step,
+replayed as a CUDA graph).  Between chunks it
+
+* retires the grids that finished (their fields are read back if asked);
+* admits waiting jobs in arrival order while the GPU has the memory for
+  them (the grid's buffer sizes from ``gmes_grid_sizes`` against
+  ``torch.cuda.mem_get_info`` minus a reserve, and an optional budget) and
+  a slot is free;
+* compiles the next jobs' scenes on the host while the chunk runs.
+
+A job's arithmetic does not depend on which other grids share its chunks,
+so its result is the same alone and in the mix.  Latency of a job =
+completion time - arrival time; the report gives p50 / p99 and the
+aggregate cell-updates per second.
+"""
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .batch import Batch
+from .engine import GridEngine, _torch
+
+
+@dataclass(order=True)
+class Job:
+    """One simulation request.
+
+    ``build`` returns an un-initialised FDTD object (the scene); ``nsteps``
+    the number of full steps to run; ``arrival`` seconds after the server
+    starts.  ``keep_fields`` reads the six fields back when the job ends.
+    """
+
+    arrival: float
+    jid: int
+    build: object = field(compare=False)
+    nsteps: int = field(compare=False)
+    keep_fields: bool = field(default=False, compare=False)
+    # filled by the server
+    scene: object = field(default=None, compare=False, repr=False)
+    engine: object = field(default=None, compare=False, repr=False)
+    done: int = field(default=0, compare=False)
+    t_admit: float = field(default=None, compare=False)
+    t_finish: float = field(default=None, compare=False)
+    fields: list = field(default=None, compare=False, repr=False)
+    error: str = field(default=None, compare=False)
+
+    @property
+    def cells(self):
+        return self.scene.cells if self.scene is not None else 0
+
+
+class Server:
+    """Resident-set FDTD server on one GPU.
+
+    ``precision``: engine precision of every job.  ``chunk``: steps per
+    chunk (<= 256).  ``max_slots``: resident grids at most.
+    ``memory_budget``: bytes the resident grids may use (default: free
+    memory at start minus ``reserve``).  ``tuner``: an ``autotune.Tuner``
+    choosing the batch launch shape, or None for the defaults.
+    """
+
+    def __init__(self, precision="fp64", chunk=64, max_slots=64, memory_budget=None,
+                 reserve=2 << 30, tuner=None, use_graphs=True, device=None):
+        torch = _torch()
+        self.precision = precision
+        self.chunk = int(chunk)
+        if not 1 <= self.chunk <= 256:
+            raise ValueError("chunk must be in [1, 256]")
+        self.max_slots = int(max_slots)
+        self.device = torch.device(device if device is not None else "cuda")
+        free, _total = torch.cuda.mem_get_info(self.device)
+        self.memory_budget = int(memory_budget if memory_budget is not None
+                                 else max(0, free - reserve))
+        self.reserve = int(reserve)
+        self.tuner = tuner
+        self.use_graphs = use_graphs
+        self.stream = torch.cuda.Stream(device=self.device)
+        self.resident = []
+        self.finished = []
+        self.failed = []
+        self.used_bytes = 0
+        self._batch = None
+        self._batch_key = None
+        self.chunks = 0
+
+    # -- admission ---------------------------------------------------------
+    @staticmethod
+    def job_bytes(scene, precision):
+        """Device bytes a grid needs (fields, maps, state, coefficients)."""
+        from . import _native as N
+        import ctypes as C
+        lib = N.load()
+        d = N.GridDescC()
+        d.abi_version = N.ABI_VERSION
+        d.precision = N.PRECISIONS[precision]
+        for a in range(3):
+            d.n[a] = scene.n[a]
+            d.dr[a] = scene.dr[a]
+        d.dt = scene.dt
+        d.active = scene.active_mask
+        for c in range(6):
+            d.naux[c] = scene.naux(c)
+            d.nclass[c] = len(scene.classes[c])
+        d.npml = len(scene.pmls)
+        d.nsrc = len(scene.sources)
+        d.nparam = sum(len(x.params) for c in range(6) for x in scene.classes[c])
+        sizes = (C.c_int64 * 21)()
+        N.check(lib.gmes_grid_sizes(C.byref(d), sizes))
+        return int(sum(sizes)) + 256 * 1024
+
+    def _fits(self, nbytes):
+        torch = _torch()
+        if self.used_bytes + nbytes > self.memory_budget:
+            return False
+        free, _ = torch.cuda.mem_get_info(self.device)
+        return nbytes + self.reserve <= free + 0  # caching allocator may hold freed blocks
+
+    def _compile(self, job):
+        if job.scene is None and job.error is None:
+            try:
+                sim = job.build()
+                job.scene = sim.compile()
+            except Exception as exc:  # a bad job fails alone
+                job.error = f"{type(exc).__name__}: {exc}"
+
+    def _admit(self, job, now):
+        self._compile(job)
+        if job.error is not None:
+            return "failed"
+        need = self.job_bytes(job.scene, self.precision)
+        if len(self.resident) >= self.max_slots or not self._fits(need):
+            return "wait"
+        try:
+            job.engine = GridEngine(job.scene, precision=self.precision, device=self.device,
+                                    src_chunk=max(self.chunk, 1), use_graphs=False)
+        except Exception as exc:
+            job.error = f"{type(exc).__name__}: {exc}"
+            return "failed"
+        job.bytes = need
+        self.used_bytes += need
+        job.t_admit = now
+        self.resident.append(job)
+        return "admitted"
+
+    def _retire(self, job, now):
+        job.t_finish = now
+        if job.keep_fields:
+            job.fields = [job.engine.read(c) for c in range(6)]
+        job.engine = None
+        self.used_bytes -= job.bytes
+        self.finished.append(job)
+
+    # -- the loop ----------------------------------------------------------
+    def _batch_for(self, jobs):
+        shape = self.tuner.choice(jobs) if self.tuner is not None else (0, 0)
+        key = (tuple(j.jid for j in jobs), shape)
+        if self._batch is None or self._batch_key != key:
+            self._batch = Batch([j.engine for j in jobs], bx_cap=shape[0], blocks=shape[1],
+                                use_graphs=self.use_graphs, stream=self.stream)
+            self._batch_key = key
+        return self._batch
+
+    def run(self, jobs, realtime=True):
+        """Serve ``jobs`` (arrival times relative to the start); return the report.
+
+        With ``realtime`` the server waits for arrivals on the wall clock;
+        otherwise a job is available as soon as the clock reaches its
+        arrival or the server is idle.
+        """
+        torch = _torch()
+        pending = sorted(jobs)
+        waiting = []
+        t0 = time.perf_counter()
+        cell_updates = 0
+        while pending or waiting or self.resident:
+            now = time.perf_counter() - t0
+            while pending and (pending[0].arrival <= now or
+                               (not realtime and not self.resident and not waiting)):
+                waiting.append(pending.pop(0))
+            # admission in arrival order; a job that does not fit blocks the
+            # ones behind it (no overtaking) unless nothing is resident
+            while waiting:
+                st = self._admit(waiting[0], now)
+                if st == "wait":
+                    break
+                job = waiting.pop(0)
+                if st == "failed":
+                    job.t_finish = now
+                    self.failed.append(job)
+            if not self.resident:
+                if waiting and not self.resident:
+                    job = waiting.pop(0)
+                    job.error = job.error or "does not fit in the memory budget"
+                    job.t_finish = now
+                    self.failed.append(job)
+                    continue
+                if pending and realtime:
+                    time.sleep(max(0.0, min(0.01, pending[0].arrival - now)))
+                continue
+            batch = self._batch_for(self.resident)
+            steps = [min(self.chunk, j.nsteps - j.done) for j in self.resident]
+            n0s = [float(j.done) for j in self.resident]
+            if self.tuner is not None:
+                self.tuner.observe_start(batch)
+            batch.run(steps, n0s)
+            # host work overlaps the chunk: compile the next arrivals' scenes
+            for job in waiting[:4]:
+                self._compile(job)
+            batch.synchronize()
+            if self.tuner is not None:
+                self.tuner.observe_end(batch, sum(s * j.cells for s, j in zip(steps, self.resident)))
+            self.chunks += 1
+            now = time.perf_counter() - t0
+            still = []
+            for j, s in zip(self.resident, steps):
+                j.done += s
+                cell_updates += s * j.cells
+                if j.done >= j.nsteps:
+                    self._retire(j, now)
+                else:
+                    still.append(j)
+            self.resident = still
+        torch.cuda.synchronize(self.device)
+        wall = time.perf_counter() - t0
+        return self.report(wall, cell_updates)
+
+    def report(self, wall, cell_updates):
+        lat = np.array([j.t_finish - j.arrival for j in self.finished], float)
+        return {
+            "jobs": len(self.finished), "failed": len(self.failed), "wall_s": wall,
+            "cell_updates": int(cell_updates),
+            "gcells_per_s": cell_updates / wall / 1e9 if wall > 0 else 0.0,
+            "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "chunks": self.chunks,
+        }
+
+
+def run_one_at_a_time(jobs, precision="fp64", device=None):
+    """The same jobs, each run alone with the plain single-grid kernels."""
+    torch = _torch()
+    t0 = time.perf_counter()
+    cell_updates = 0
+    for job in sorted(jobs):
+        sim = job.build()
+        scene = sim.compile()
+        eng = GridEngine(scene, precision=precision, device=device, use_graphs=False)
+        eng.step(job.nsteps)
+        eng.synchronize()
+        cell_updates += job.nsteps * scene.cells
+        if job.keep_fields:
+            job.fields = [eng.read(c) for c in range(6)]
+        del eng
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return {"wall_s": wall, "cell_updates": cell_updates,
+            "gcells_per_s": cell_updates / wall / 1e9}

@@ -116,3 +116,57 @@ def bytes_per_cell_update(scene, precision):
         for cid, cnt in counts.items():
             total += 2 * naux_of(scene.classes[c][cid]) * es * cnt
     return total
+
+
+def serving_jobs(njobs=512, seed=0, rate=None, max_steps=5000, min_steps=500, size_scale=1.0,
+                 precision="fp64"):
+    """The batched-serving request stream: (arrival, build, nsteps) triples.
+
+    Half the jobs are 2-D TMz grids with side uniform in [128, 1024], half
+    3-D grids with side uniform in [64, 160] (times ``size_scale``); the
+    medium of a central sphere is drawn from {dielectric eps in [1, 12],
+    Drude (omega_p 9, gamma 0.07), Lorentz (2.0, 3.0, 0.1)}; CPML 8-16
+    cells; step counts uniform in [min_steps, max_steps]; Poisson arrivals
+    with ``rate`` jobs per second (default: all at once).
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    t = 0.0
+    for q in range(njobs):
+        if rate:
+            t += float(rng.exponential(1.0 / rate))
+        three_d = q % 2 == 1
+        side = int(round((rng.uniform(64, 160) if three_d else rng.uniform(128, 1024))
+                         * size_scale))
+        side = max(side, 24)
+        pml = int(rng.integers(8, 17))
+        kind = int(rng.integers(0, 3))
+        eps = float(rng.uniform(1.0, 12.0))
+        nsteps = int(rng.integers(min_steps, max_steps + 1))
+        out.append((t, _serving_builder(side, three_d, pml, kind, eps, precision), nsteps))
+    return out
+
+
+def _serving_builder(side, three_d, pml, kind, eps, precision):
+    def build():
+        res = 10
+        dx = 1.0 / res
+        size = side * dx
+        if kind == 0:
+            mat = Dielectric(eps_inf=eps)
+        elif kind == 1:
+            mat = Drude(eps_inf=1, dps=(DrudePole(omega=9.0, gamma=0.07),))
+        else:
+            mat = Lorentz(lps=(LorentzPole(amp=2.0, omega=3.0, gamma=0.1),))
+        r = 0.25 * (size / 2 - pml * dx)
+        geom = [DefaultMedium(material=Dielectric()),
+                Sphere(material=mat, center=(0.3 * r, 0, 0), radius=r),
+                Shell(material=Cpml(), thickness=pml * dx)]
+        src = [PointSource(src_time=Bandpass(freq=0.8, fwidth=0.5), center=(-r, 0, 0),
+                           component=Ez)]
+        if three_d:
+            space = Cartesian(size=(size, size, size), resolution=res)
+            return FDTD(space, geom, src, verbose=False, precision=precision)
+        space = Cartesian(size=(size, size, 0), resolution=res)
+        return TMzFDTD(space, geom, src, verbose=False, precision=precision)
+    return build

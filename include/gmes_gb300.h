@@ -228,6 +228,59 @@ gmes_status gmes_step(const gmes_grid_desc* g, int32_t nsteps, void* stream);
  */
 gmes_status gmes_half_step(const gmes_grid_desc* g, int32_t side, int32_t step, void* stream);
 
+/*
+ * Batches: several grids (jobs) advanced together, one launch per kernel
+ * kind per half-step for the whole batch (the serving path).  The caller
+ * allocates a device workspace of gmes_batch_workspace_size(njobs) bytes;
+ * gmes_batch_prepare() writes the per-grid views and work prefix sums into
+ * it and fills *out.  All grids of a batch share one precision and must not
+ * be stepped through any other call while the batch runs.  No reference
+ * counterpart: the reference runs one simulation per process.
+ */
+typedef struct {
+  int32_t njobs;
+  int32_t precision;
+  int32_t dispersive;    /* some grid has GMES_FLAG_DISPERSIVE */
+  int32_t srcs;          /* point sources over all grids */
+  int64_t tiles;         /* blocks of one half-step over all grids */
+  int64_t ghosts;        /* ghost-copy work items over all grids */
+  void* workspace;       /* device */
+  int64_t workspace_bytes;
+} gmes_batch;
+
+int64_t gmes_batch_workspace_size(int32_t njobs);
+
+/* bx_cap: log2 of the largest block extent along k (0..5; 0 = default 5). */
+gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs,
+                               void* workspace, int64_t workspace_bytes, int32_t bx_cap,
+                               gmes_batch* out, void* stream);
+
+/*
+ * Steps each grid takes in the next chunk: host array of njobs, copied in
+ * stream order (it must stay valid until the stream reaches the copy).
+ */
+gmes_status gmes_batch_set_steps(const gmes_batch* b, const int32_t* steps, void* stream);
+
+/*
+ * Advance a chunk of nsteps steps: grid g takes steps 0 .. steps[g]-1 of
+ * the chunk, reading its source values from its own src_val at those step
+ * slots.  blocks: grid size of the persistent update kernel (0 = one block
+ * per tile).
+ */
+gmes_status gmes_batch_step(const gmes_batch* b, int32_t nsteps, int32_t blocks, void* stream);
+
+/*
+ * CUDA graphs of whole chunks (stream capture of gmes_step / gmes_batch_step
+ * on a non-default stream).  The graph bakes in the descriptors' device
+ * pointers: replay it only while the same buffers are alive.
+ */
+gmes_status gmes_graph_capture_step(const gmes_grid_desc* g, int32_t nsteps, void* stream,
+                                    void** graph_exec);
+gmes_status gmes_graph_capture_batch(const gmes_batch* b, int32_t nsteps, int32_t blocks,
+                                     void* stream, void** graph_exec);
+gmes_status gmes_graph_launch(void* graph_exec, void* stream);
+gmes_status gmes_graph_destroy(void* graph_exec);
+
 /* Copy a component between host and device memory (numpy <-> GPU). */
 gmes_status gmes_read_field(const gmes_grid_desc* g, int32_t comp, double* host_out,
                             void* stream);
