@@ -165,7 +165,7 @@ def ncu_traffic(workload_key, precision):
 # ---------------------------------------------------------------------------
 # algorithmic bytes
 # ---------------------------------------------------------------------------
-def half_bytes(scene, precision):
+def half_bytes(scene, precision, engine=None):
     """Algorithmic DRAM bytes of each half-step: (E half, H half).
 
     E half: read+write every E value, read every H value, read the E class
@@ -182,7 +182,8 @@ def half_bytes(scene, precision):
             npts = int(np.prod(scene.shape(c)))
             if (c < 3) == (side == 0):
                 b += 2 * es * npts + npts
-                for cid, cnt in scene.counts(c).items():
+                counts = engine.class_counts(c) if engine is not None else scene.counts(c)
+                for cid, cnt in counts.items():
                     b += 2 * naux_of(scene.classes[c][cid]) * es * cnt
             else:
                 b += es * npts
@@ -320,7 +321,7 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = cells * args.steps * world / (total_ms / 1e3) / 1e9
-    eb, hb = half_bytes(scene, args.precision)
+    eb, hb = half_bytes(scene, args.precision, sim.engine)
     dom = ("E half-step", eb, e_ms) if e_ms >= h_ms else ("H half-step", hb, h_ms)
     peak, peak_src = measured_peak()
     achieved = dom[1] / (dom[2] / 1e3) / 1e9
@@ -356,7 +357,7 @@ def run_ours(args):
                 vs.init()
                 vk = min(args.steps, 100)
                 t_ms, ve, vh, _ = timed_loop(vs, vk, 5, lambda: None)
-                veb, vhb = half_bytes(vs.scene, prec)
+                veb, vhb = half_bytes(vs.scene, prec, vs.engine)
                 vdom = (veb, ve) if ve >= vh else (vhb, vh)
                 result["variants"][prec] = {
                     "value": round(cells * vk / (t_ms / 1e3) / 1e9, 4),

@@ -26,7 +26,7 @@ EXPORTS = [
     "gmes_step", "gmes_half_step", "gmes_read_field", "gmes_write_field",
     "gmes_batch_workspace_size", "gmes_batch_prepare", "gmes_batch_set_steps", "gmes_batch_step",
     "gmes_graph_capture_step", "gmes_graph_capture_batch", "gmes_graph_launch",
-    "gmes_graph_destroy",
+    "gmes_graph_destroy", "gmes_rasterize",
 ]
 
 
@@ -57,6 +57,17 @@ class GridDescC(C.Structure):
         ("field", C.c_void_p * 6), ("cls", C.c_void_p * 6), ("aux", C.c_void_p * 6),
         ("coef", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p),
     ]
+
+
+class ShapeC(C.Structure):
+    _fields_ = [("type", C.c_int32), ("compound", C.c_int32), ("nbox", C.c_int32),
+                ("pad", C.c_int32), ("lo", C.c_double * 3), ("hi", C.c_double * 3),
+                ("center", C.c_double * 3), ("m", C.c_double * 9), ("p", C.c_double * 3),
+                ("axis", C.c_double * 3), ("box_lo", (C.c_double * 3) * 6),
+                ("box_hi", (C.c_double * 3) * 6)]
+
+
+SHAPE_ALL, SHAPE_SPHERE, SHAPE_BLOCK, SHAPE_ELLIPSOID, SHAPE_CONE, SHAPE_SHELL = range(6)
 
 
 class BatchC(C.Structure):
@@ -112,6 +123,8 @@ def load():
     lib.gmes_graph_capture_batch.argtypes = [P(BatchC), C.c_int32, C.c_int32, C.c_void_p,
                                              P(C.c_void_p)]
     lib.gmes_graph_launch.argtypes = [C.c_void_p, C.c_void_p]
+    lib.gmes_rasterize.argtypes = [P(GridDescC), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                                   C.c_void_p]
     lib.gmes_graph_destroy.argtypes = [C.c_void_p]
     for name in EXPORTS:
         if name not in ("gmes_abi_version", "gmes_last_error", "gmes_elem_size",

@@ -22,10 +22,10 @@ LIB = PKG / "libgmes_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           f"-I{ROOT / 'include'}"]
-# Per-file flags: the coefficient builder reproduces the reference's FP64
-# operation order, so multiply-add contraction is disabled there.
-EXTRA = {"gmes_coef.cu": ["--fmad=false"]}
-SOURCES = ["gmes_capi.cu", "gmes_coef.cu", "gmes_step.cu"]
+# Per-file flags: the coefficient builder and the rasteriser reproduce the
+# reference's FP64 operation order, so multiply-add contraction is disabled.
+EXTRA = {"gmes_coef.cu": ["--fmad=false"], "gmes_raster.cu": ["--fmad=false"]}
+SOURCES = ["gmes_capi.cu", "gmes_coef.cu", "gmes_step.cu", "gmes_raster.cu"]
 
 
 def nvcc():

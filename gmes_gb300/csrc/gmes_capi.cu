@@ -541,6 +541,22 @@ gmes_status gmes_graph_destroy(void* graph_exec) {
   return GMES_OK;
 }
 
+gmes_status gmes_rasterize(const gmes_grid_desc* g, int32_t comp, const gmes_shape* shapes,
+                           int32_t nshapes, const uint8_t* lut, void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  if (comp < 0 || comp > 5) return fail(GMES_ERR_INDEX, "component %d outside [0, 5]", comp);
+  if (!((g->active >> comp) & 1)) return fail(GMES_ERR_VALUE, "component %d inactive", comp);
+  if (shapes == nullptr || lut == nullptr) return fail(GMES_ERR_VALUE, "NULL shapes or lut");
+  if (nshapes < 1 || nshapes > 255)
+    return fail(GMES_ERR_VALUE, "nshapes = %d outside [1, 255]", nshapes);
+  const GridDev d = make_grid_dev(*g);
+  cudaError_t e = launch_raster(*g, d, comp, shapes, nshapes, lut,
+                                static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching the rasteriser");
+  return GMES_OK;
+}
+
 gmes_status gmes_read_field(const gmes_grid_desc* g, int32_t comp, double* host_out,
                             void* stream) {
   gmes_status st = check_desc(g, true);

@@ -268,6 +268,9 @@ cudaError_t launch_half(const gmes_grid_desc& g, const GridDev& d, int side, int
                         cudaStream_t s);
 cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nsteps, int blocks,
                          cudaStream_t s);
+cudaError_t launch_raster(const gmes_grid_desc& gd, const GridDev& d, int c,
+                          const gmes_shape* shapes, int nshapes, const uint8_t* lut,
+                          cudaStream_t s);
 cudaError_t launch_build_coefficients(const gmes_grid_desc& g, const GridDev& d,
                                       cudaStream_t s);
 

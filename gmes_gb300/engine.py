@@ -89,8 +89,11 @@ class GridEngine:
             else:
                 a = None
             self.aux.append(a)
-            if scene.cls[c] is not None:
-                m = torch.from_numpy(scene.cls[c]).to(dev)
+            if (scene.active_mask >> c) & 1:
+                if scene.cls[c] is not None or not scene.device_raster:
+                    m = torch.from_numpy(scene.host_cls(c)).to(dev)
+                else:
+                    m = torch.zeros(shape, dtype=torch.uint8, device=dev)  # rasterised below
                 d.cls[c] = m.data_ptr()
             else:
                 m = None
@@ -118,6 +121,10 @@ class GridEngine:
         self._stream = torch.cuda.Stream(device=dev)
         self._enter()
         self.build_coefficients()
+        self.rasterized = False
+        if scene.device_raster and any(scene.cls[c] is None for c in range(6)
+                                       if (scene.active_mask >> c) & 1):
+            self._rasterize()
         self._leave()
 
     def __del__(self):
@@ -169,6 +176,52 @@ class GridEngine:
                                                       p["a_max"], p["d"])
         N.check(self.lib.gmes_build_coefficients(C.byref(self.desc), crow, cpool, cpml,
                                                  C.c_void_p(self.stream)))
+
+    def _rasterize(self):
+        """Build the class maps of the components not given on the host (on the GPU)."""
+        torch = _torch()
+        scene = self.scene
+        recs = scene.shapes
+        arr = (N.ShapeC * len(recs))()
+        for q, r in enumerate(recs):
+            sh = arr[q]
+            sh.type = r["type"]
+            sh.compound = r["compound"]
+            sh.nbox = r.get("nbox", 0)
+            for a in range(3):
+                sh.lo[a] = r["lo"][a]
+                sh.hi[a] = r["hi"][a]
+                sh.center[a] = r.get("center", [0.0] * 3)[a]
+                sh.p[a] = r.get("p", [0.0] * 3)[a]
+                sh.axis[a] = r.get("axis", [0.0] * 3)[a]
+            for t, v in enumerate(r.get("m", [0.0] * 9)):
+                sh.m[t] = v
+            for b, (lo, hi) in enumerate(zip(r.get("box_lo", []), r.get("box_hi", []))):
+                for a in range(3):
+                    sh.box_lo[b][a] = lo[a]
+                    sh.box_hi[b][a] = hi[a]
+        with torch.cuda.stream(self._stream):
+            shapes = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
+            for c in range(6):
+                if not (scene.active_mask >> c) & 1 or scene.cls[c] is not None:
+                    continue
+                lut = torch.from_numpy(np.ascontiguousarray(scene.lut[c])).to(self.device)
+                N.check(self.lib.gmes_rasterize(C.byref(self.desc), c,
+                                                C.c_void_p(shapes.data_ptr()), len(recs),
+                                                C.c_void_p(lut.data_ptr()),
+                                                C.c_void_p(self.stream)))
+                self._raster_keep = (shapes, lut)
+            self._stream.synchronize()
+        self.rasterized = True
+
+    def class_counts(self, c):
+        """Points per class of component ``c``, counted on the GPU."""
+        m = self.cls[c]
+        if m is None:
+            return {}
+        self._leave()
+        cnt = _torch().bincount(m.view(-1).long(), minlength=len(self.scene.classes[c]))
+        return {i: int(v) for i, v in enumerate(cnt.tolist()) if v}
 
     def set_pml_profile(self, pml, comp, axis, values):
         self._enter()

@@ -220,7 +220,7 @@ class FDTD:
             c = comp.index
             out = {}
             per_kind = {}
-            for cls_id, count in self._scene.counts(c).items():
+            for cls_id, count in self._engine.class_counts(c).items():
                 kind = self._scene.classes[c][cls_id].kind
                 per_kind[kind] = per_kind.get(kind, 0) + count
             for kind, count in per_kind.items():

@@ -320,6 +320,16 @@ class GeometricObject:
         """Vectorised inclusion test over broadcastable coordinate arrays."""
         raise NotImplementedError
 
+    def shape_record(self):
+        """Fields of this shape's ``gmes_shape`` for the GPU rasteriser."""
+        raise NotImplementedError
+
+    def _record(self, kind, **kw):
+        rec = {"type": kind, "compound": int(getattr(self.material, "compound", False)),
+               "lo": [float(v) for v in self.box.low], "hi": [float(v) for v in self.box.high]}
+        rec.update(kw)
+        return rec
+
     def display_info(self, indent=0):
         if self.material:
             self.material.display_info(indent + 5)
@@ -333,6 +343,9 @@ class DefaultMedium(GeometricObject):
 
     def contains(self, x, y, z):
         return np.ones(np.broadcast_shapes(np.shape(x), np.shape(y), np.shape(z)), bool)
+
+    def shape_record(self):
+        return self._record(0)
 
 
 class Cone(GeometricObject):
@@ -362,6 +375,10 @@ class Cone(GeometricObject):
         px, py, pz = rx - proj * ax[0], ry - proj * ax[1], rz - proj * ax[2]
         dist = np.sqrt(px ** 2 + py ** 2 + pz ** 2)
         return inside & (dist <= np.abs(radius))
+
+    def shape_record(self):
+        return self._record(4, center=list(self.center), axis=list(self.axis),
+                            p=[self.radius, self.radius2, self.height])
 
     def geom_box(self):
         h = 0.5 * self.height
@@ -406,6 +423,11 @@ class Block(GeometricObject):
         h = 0.5 * self.size
         return (np.abs(p[0]) <= h[0]) & (np.abs(p[1]) <= h[1]) & (np.abs(p[2]) <= h[2])
 
+    def shape_record(self):
+        return self._record(2, center=list(self.center),
+                            m=[float(v) for v in self.projection_matrix.ravel()],
+                            p=[float(v) for v in 0.5 * self.size])
+
     def geom_box(self):
         s1, s2, s3 = self.size[0] * self.e1, self.size[1] * self.e2, self.size[2] * self.e3
         corner = self.center - 0.5 * (s1 + s2 + s3)
@@ -429,6 +451,11 @@ class Ellipsoid(Block):
         q = [p[a] * self.inverse_semi_axes[a] for a in range(3)]
         return (q[0] * q[0] + q[1] * q[1]) + q[2] * q[2] <= 1
 
+    def shape_record(self):
+        return self._record(3, center=list(self.center),
+                            m=[float(v) for v in self.projection_matrix.ravel()],
+                            p=[float(v) for v in self.inverse_semi_axes])
+
 
 class Sphere(GeometricObject):
     """Sphere (src/pygeom.pyx:897-973): |p - center| <= radius."""
@@ -446,6 +473,9 @@ class Sphere(GeometricObject):
 
     def geom_box(self):
         return GeomBox(self.center - self.radius, self.center + self.radius)
+
+    def shape_record(self):
+        return self._record(1, center=list(self.center), p=[self.radius, 0.0, 0.0])
 
 
 class Shell(GeometricObject):
@@ -511,6 +541,11 @@ class Shell(GeometricObject):
 
     def geom_box(self):
         return GeomBox(self.center - self.half_size, self.center + self.half_size)
+
+    def shape_record(self):
+        return self._record(5, nbox=len(self.box_list),
+                            box_lo=[[float(v) for v in b.low] for b in self.box_list],
+                            box_hi=[[float(v) for v in b.high] for b in self.box_list])
 
 
 class GeomBoxTree:

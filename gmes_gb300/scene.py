@@ -39,10 +39,15 @@ class Scene:
     """Everything the engine needs to advance one grid.
 
     Attributes: ``n`` (whole_field_size), ``active`` (tuple of active
-    component classes, E first), ``dr``, ``half``, ``dt``, ``cls`` (list of 6
-    uint8 arrays or None), ``classes`` (list of 6 lists of ClassDesc; class
-    0 is always Dummy), ``pmls`` (list of PML material objects), ``sources``
-    (list of PointSourceSpec).
+    component classes, E first), ``dr``, ``half``, ``dt``, ``classes`` (list
+    of 6 lists of ClassDesc; class 0 is always Dummy), ``pmls`` (list of PML
+    material objects), ``sources`` (list of PointSourceSpec).
+
+    Class maps: ``lut[c]`` maps (owner shape, underneath shape + 1) to a
+    class id, and ``shapes`` holds the rasteriser records of the geometry
+    list, so the engine can build the u8 class maps on the GPU
+    (``gmes_rasterize``).  ``host_cls(c)`` builds the same map on the host
+    (numpy); ``cls[c]`` caches it.
     """
 
     def __init__(self, n, active, dr, half, dt):
@@ -52,9 +57,13 @@ class Scene:
         self.half = tuple(float(v) for v in half)
         self.dt = float(dt)
         self.cls = [None] * 6
+        self.lut = [None] * 6
         self.classes = [[] for _ in range(6)]
         self.pmls = []
         self.sources = []
+        self.shapes = None
+        self._geom = None
+        self._space = None
 
     @property
     def active_mask(self):
@@ -82,6 +91,11 @@ class Scene:
     def cells(self):
         return int(np.prod(self.n))
 
+    @property
+    def device_raster(self):
+        """True when the class maps can be built on the GPU."""
+        return self.shapes is not None
+
     def pml_index(self, pml):
         for i, p in enumerate(self.pmls):
             if p is pml:
@@ -89,11 +103,24 @@ class Scene:
         self.pmls.append(pml)
         return len(self.pmls) - 1
 
+    def host_cls(self, c):
+        """u8 class map of component ``c`` rasterised on the host."""
+        if self.cls[c] is None and (self.active_mask >> c) & 1:
+            comp = next(a for a in self.active if a.index == c)
+            shape = self.shape(c)
+            coords = [self._space.axis_coords(comp, a, shape[a]) for a in range(3)]
+            owner, under = rasterize(self._geom, coords)
+            m = self.lut[c][owner.astype(np.intp), under.astype(np.intp) + 1]
+            _edge_dummy(m, c)
+            self.cls[c] = np.ascontiguousarray(m, np.uint8)
+        return self.cls[c]
+
     def counts(self, c):
         """Points per class of component ``c`` (the reference's idx_size())."""
-        if self.cls[c] is None:
+        m = self.host_cls(c)
+        if m is None:
             return {}
-        cnt = np.bincount(self.cls[c].ravel(), minlength=len(self.classes[c]))
+        cnt = np.bincount(m.ravel(), minlength=len(self.classes[c]))
         return {i: int(v) for i, v in enumerate(cnt) if v}
 
 
@@ -106,29 +133,22 @@ def _edge_dummy(cls, c):
         cls[tuple(sl)] = 0
 
 
-def compile_scene(space, geom_list, e_comps, h_comps, src_list, geom_tree, dt):
-    active = tuple(e_comps) + tuple(h_comps)
-    scene = Scene(space.whole_field_size, active, space.dr, space.half_size, dt)
+def _class_table(geom_list, comp, scene):
+    """Class descriptors and the (owner, under + 1) -> class id table of one component.
+
+    Every possible pair is numbered: a non-compound owner with under = -1,
+    a compound owner (a PML) with each earlier shape as underneath
+    (src/pygeom.pyx:425-441).  Distinct descriptors share an id.
+    """
     G = len(geom_list)
-    for comp in active:
-        c = comp.index
-        shape = scene.shape(c)
-        coords = [space.axis_coords(comp, a, shape[a]) for a in range(3)]
-        owner, under = rasterize(geom_list, coords)
-        code = owner.astype(np.int32) * (G + 1) + (under.astype(np.int32) + 1)
-        present = np.zeros(G * (G + 1) + G + 1, bool)
-        present[code.ravel()] = True
-        lut = np.zeros(len(present), np.uint8)
-        descs = [ClassDesc(KIND_DUMMY, 1.0)]
-        keys = {}
-        for cc in np.nonzero(present)[0]:
-            m, u = divmod(int(cc), G + 1)
-            u -= 1
-            mat = geom_list[m].material
-            underneath = geom_list[u].material if u >= 0 else None
-            desc = mat.engine_class(comp, underneath)
-            if desc.pml is not None:
-                scene.pml_index(desc.pml)
+    descs = [ClassDesc(KIND_DUMMY, 1.0)]
+    keys = {}
+    lut = np.zeros((G, G + 1), np.uint8)
+    for m in range(G):
+        mat = geom_list[m].material
+        compound = getattr(mat, "compound", False) and m > 0
+        for u in (range(m) if compound else (-1,)):
+            desc = mat.engine_class(comp, geom_list[u].material if u >= 0 else None)
             k = desc.key()
             if k not in keys:
                 if len(descs) >= MAX_CLASSES:
@@ -136,11 +156,31 @@ def compile_scene(space, geom_list, e_comps, h_comps, src_list, geom_tree, dt):
                                      f"on component {comp.__name__}")
                 keys[k] = len(descs)
                 descs.append(desc)
-            lut[cc] = keys[k]
-        cls = lut[code]
-        _edge_dummy(cls, c)
-        scene.cls[c] = np.ascontiguousarray(cls)
-        scene.classes[c] = descs
+                if desc.pml is not None:
+                    scene.pml_index(desc.pml)
+            lut[m, u + 1] = keys[k]
+    return descs, lut
+
+
+def compile_scene(space, geom_list, e_comps, h_comps, src_list, geom_tree, dt):
+    """Class tables, rasteriser records and point sources of a scene.
+
+    No per-point work happens here: the class maps are built on the GPU by
+    the engine, or on the host on demand (``Scene.host_cls``).
+    """
+    active = tuple(e_comps) + tuple(h_comps)
+    scene = Scene(space.whole_field_size, active, space.dr, space.half_size, dt)
+    scene._geom = list(geom_list)
+    scene._space = space
+    for comp in active:
+        descs, lut = _class_table(geom_list, comp, scene)
+        scene.classes[comp.index] = descs
+        scene.lut[comp.index] = lut
+    try:
+        recs = [g.shape_record() for g in geom_list]
+        scene.shapes = recs if 1 <= len(recs) <= 255 else None
+    except NotImplementedError:
+        scene.shapes = None
     # point sources: a later source at the same point replaces an earlier
     # one, as PwSource.attach/merge do (gmes/pw_source.py:25-36)
     specs = {}

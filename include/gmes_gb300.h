@@ -281,6 +281,39 @@ gmes_status gmes_graph_capture_batch(const gmes_batch* b, int32_t nsteps, int32_
 gmes_status gmes_graph_launch(void* graph_exec, void* stream);
 gmes_status gmes_graph_destroy(void* graph_exec);
 
+/*
+ * Material-map builder on the GPU (replaces the per-point Python loop of
+ * FDTD.init_material_*, gmes/fdtd.py:353-477, and the geometry tree lookups
+ * of src/pygeom.pyx:300-454).  Every point of component `comp` takes the
+ * LAST shape of the list that contains it (shape 0 when none of shapes
+ * 1.. does: find_object, src/pygeom.pyx:143-156); for a compound owner
+ * (a PML) the "underneath" shape is the last earlier shape containing the
+ * point.  The class id written is lut[owner * (nshapes + 1) + under + 1]
+ * (under = -1 for a non-compound owner); ghost planes get class 0.
+ * shapes and lut are DEVICE arrays.  Inclusion tests use the reference's
+ * FP64 arithmetic (src/pygeom.pyx:538-1148) without multiply-add fusion.
+ */
+enum { GMES_SHAPE_ALL = 0, GMES_SHAPE_SPHERE = 1, GMES_SHAPE_BLOCK = 2,
+       GMES_SHAPE_ELLIPSOID = 3, GMES_SHAPE_CONE = 4, GMES_SHAPE_SHELL = 5 };
+
+typedef struct {
+  int32_t type;         /* GMES_SHAPE_* */
+  int32_t compound;     /* 1: the shape's material takes eps/mu from underneath */
+  int32_t nbox;         /* SHELL: slab boxes in box_lo/box_hi */
+  int32_t pad;
+  double lo[3], hi[3];  /* bounding box (inclusive); a point outside is not inside */
+  double center[3];
+  double m[9];          /* BLOCK/ELLIPSOID: projection onto the edge axes, row-major */
+  double p[3];          /* SPHERE: radius; BLOCK: half sizes; ELLIPSOID: 2 / sizes;
+                           CONE: radius, radius2, height */
+  double axis[3];       /* CONE: unit axis */
+  double box_lo[6][3];  /* SHELL slabs */
+  double box_hi[6][3];
+} gmes_shape;
+
+gmes_status gmes_rasterize(const gmes_grid_desc* g, int32_t comp, const gmes_shape* shapes,
+                           int32_t nshapes, const uint8_t* lut, void* stream);
+
 /* Copy a component between host and device memory (numpy <-> GPU). */
 gmes_status gmes_read_field(const gmes_grid_desc* g, int32_t comp, double* host_out,
                             void* stream);

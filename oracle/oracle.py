@@ -105,8 +105,8 @@ class Oracle:
                     raise ValueError("bad class")
                 k += 1
         for c in range(6):
-            if scene.cls[c] is not None:
-                m = np.ascontiguousarray(scene.cls[c], np.uint8)
+            if (scene.active_mask >> c) & 1:
+                m = np.ascontiguousarray(scene.host_cls(c), np.uint8)
                 if self.lib.oracle_set_class_map(self.h, c,
                                                  m.ctypes.data_as(C.POINTER(C.c_uint8))) != 0:
                     raise ValueError("bad class map")
