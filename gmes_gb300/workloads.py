@@ -139,7 +139,7 @@ def serving_jobs(njobs=512, seed=0, rate=None, max_steps=5000, min_steps=500, si
         side = int(round((rng.uniform(64, 160) if three_d else rng.uniform(128, 1024))
                          * size_scale))
         side = max(side, 24)
-        pml = int(rng.integers(8, 17))
+        pml = min(int(rng.integers(8, 17)), side // 4)
         kind = int(rng.integers(0, 3))
         eps = float(rng.uniform(1.0, 12.0))
         nsteps = int(rng.integers(min_steps, max_steps + 1))
