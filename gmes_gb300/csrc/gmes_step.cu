@@ -91,12 +91,19 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
     // psi stays exactly 0 (b * 0 + 0 * D), so its update is skipped.
     const Coef* q1 = g.prof[__ldg(&cc.pml)][C][a1] + (int64_t)x[a1] * kProfStride;
     const Coef* q2 = g.prof[__ldg(&cc.pml)][C][a2] + (int64_t)x[a2] * kProfStride;
+    const bool on1 = coef_nonzero(q1 + 1), on2 = coef_nonzero(q2 + 1);
+    if (!on1 && !on2) {
+      // outside both slabs kappa = 1 and psi = 0: the dielectric update
+      const R c1 = P::cfg(&cc.c1), c2 = P::cfg(&cc.c2);
+      P::st(fp, E ? (F + c1 * p1) - c2 * p2 : (F + c2 * p2) - c1 * p1);
+      return;
+    }
     R psi1 = pre.a, psi2 = pre.b;
-    if (coef_nonzero(q1 + 1)) {
+    if (on1) {
       psi1 = P::cfg(q1) * psi1 + P::cfg(q1 + 3) * p1;
       P::st(aux + lin, psi1);
     }
-    if (coef_nonzero(q2 + 1)) {
+    if (on2) {
       psi2 = P::cfg(q2) * psi2 + P::cfg(q2 + 3) * p2;
       P::st(aux + np + lin, psi2);
     }
