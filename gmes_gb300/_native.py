@@ -26,8 +26,9 @@ EXPORTS = [
     "gmes_step", "gmes_half_step", "gmes_read_field", "gmes_write_field",
     "gmes_batch_workspace_size", "gmes_batch_prepare", "gmes_batch_set_steps", "gmes_batch_step",
     "gmes_graph_capture_step", "gmes_graph_capture_batch", "gmes_graph_launch",
-    "gmes_graph_destroy", "gmes_rasterize",
+    "gmes_graph_destroy", "gmes_rasterize", "gmes_batch_step_noalloc",
 ]
+NOALLOC_MAX_GRIDS = 64
 
 
 class ClassDescC(C.Structure):
@@ -123,6 +124,8 @@ def load():
     lib.gmes_graph_capture_batch.argtypes = [P(BatchC), C.c_int32, C.c_int32, C.c_void_p,
                                              P(C.c_void_p)]
     lib.gmes_graph_launch.argtypes = [C.c_void_p, C.c_void_p]
+    lib.gmes_batch_step_noalloc.argtypes = [P(P(GridDescC)), P(C.c_int32), C.c_int32,
+                                            C.c_int32, C.c_int32, C.c_void_p]
     lib.gmes_rasterize.argtypes = [P(GridDescC), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                    C.c_void_p]
     lib.gmes_graph_destroy.argtypes = [C.c_void_p]

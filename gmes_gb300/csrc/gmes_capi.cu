@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <functional>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -621,3 +622,103 @@ gmes_status gmes_write_field(const gmes_grid_desc* g, int32_t comp, const double
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// gmes_batch_step_noalloc: the batch tables in a fixed device array.
+// ---------------------------------------------------------------------------
+namespace gmes {
+namespace {
+
+constexpr int64_t kNoAllocBytes = 192 * 1024;  // >= batch_layout(GMES_NOALLOC_MAX_GRIDS).total
+static_assert(GMES_NOALLOC_MAX_GRIDS * sizeof(GridDev) + 8192 <= kNoAllocBytes,
+              "fixed batch table too small for GMES_NOALLOC_MAX_GRIDS grids");
+
+// The batch tables of gmes_batch_step_noalloc.  Host code never touches this
+// symbol directly: its device address comes from cudaGetSymbolAddress.
+__device__ __align__(256) char g_noalloc_tables[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kMaxDevices] = {};          // per device, looked up on first use
+alignas(256) char g_noalloc_image[kNoAllocBytes];  // host image, guarded by the mutex
+
+}  // namespace
+}  // namespace gmes
+
+extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grids,
+                                               const int32_t* steps, int32_t njobs,
+                                               int32_t nsteps, int32_t bx_cap, void* stream) {
+  if (grids == nullptr || steps == nullptr) return fail(GMES_ERR_VALUE, "NULL argument");
+  if (njobs < 1 || njobs > GMES_NOALLOC_MAX_GRIDS)
+    return fail(GMES_ERR_VALUE, "njobs = %d outside [1, %d] (the fixed table's capacity)",
+                njobs, GMES_NOALLOC_MAX_GRIDS);
+  if (nsteps < 0) return fail(GMES_ERR_VALUE, "nsteps = %d must be >= 0", nsteps);
+  if (bx_cap < 0 || bx_cap > 5) return fail(GMES_ERR_VALUE, "bx_cap = %d outside [0, 5]", bx_cap);
+  if (bx_cap == 0) bx_cap = 5;
+  const BatchLayout L = batch_layout(njobs);
+  if (L.total > kNoAllocBytes)
+    return fail(GMES_ERR_RUNTIME, "batch tables of %lld bytes exceed the fixed %lld",
+                (long long)L.total, (long long)kNoAllocBytes);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(GMES_ERR_RUNTIME, "device %d unsupported", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* addr = nullptr;
+    e = cudaGetSymbolAddress(&addr, g_noalloc_tables);
+    if (e != cudaSuccess) return cuda_fail(e, "looking up the fixed batch table");
+    g_noalloc_addr[dev] = addr;
+  }
+  char* img = g_noalloc_image;
+  std::memset(img, 0, (size_t)L.total);
+  GridDev* jobs = reinterpret_cast<GridDev*>(img + L.jobs);
+  int64_t* tp = reinterpret_cast<int64_t*>(img + L.tile_prefix);
+  int32_t* bxl = reinterpret_cast<int32_t*>(img + L.bxl);
+  int32_t* stp = reinterpret_cast<int32_t*>(img + L.steps);
+  int64_t* gp = reinterpret_cast<int64_t*>(img + L.ghost_prefix);
+  int32_t* sp = reinterpret_cast<int32_t*>(img + L.src_prefix);
+  int32_t precision = -1;
+  bool disp = false;
+  for (int q = 0; q < njobs; ++q) {
+    const gmes_grid_desc* g = grids[q];
+    gmes_status st = check_desc(g, true);
+    if (st != GMES_OK) return st;
+    if (precision < 0) precision = g->precision;
+    if (g->precision != precision)
+      return fail(GMES_ERR_VALUE, "grid %d: all grids must share one precision", q);
+    if (steps[q] < 0 || steps[q] > nsteps)
+      return fail(GMES_ERR_VALUE, "steps[%d] = %d outside [0, nsteps]", q, steps[q]);
+    if (g->nsrc > 0 && steps[q] > g->src_steps)
+      return fail(GMES_ERR_VALUE, "steps[%d] exceeds the grid's source-value capacity", q);
+    disp = disp || (g->flags & GMES_FLAG_DISPERSIVE);
+    jobs[q] = make_grid_dev(*g);
+    int l = 0;
+    while (l < bx_cap && (1 << l) < g->n[2]) ++l;
+    bxl[q] = l;
+    const int64_t bx = 1 << l, by = kBatchThreads / bx;
+    const int64_t tiles = ((g->n[2] + bx - 1) / bx) * ((g->n[1] + by - 1) / by) * g->n[0];
+    tp[q + 1] = tp[q] + tiles;
+    gp[q + 1] = gp[q] + 6 * max_ghost_plane(jobs[q]);
+    sp[q + 1] = sp[q] + g->nsrc;
+    stp[q] = steps[q];
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // pageable source: the call returns once the image is staged, so the host
+  // image can be rebuilt by the next call
+  e = cudaMemcpyAsync(g_noalloc_addr[dev], img, (size_t)L.total, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "uploading the fixed batch table");
+  gmes_batch b;
+  b.njobs = njobs;
+  b.precision = precision;
+  b.dispersive = disp ? 1 : 0;
+  b.srcs = sp[njobs];
+  b.tiles = tp[njobs];
+  b.ghosts = gp[njobs];
+  b.workspace = g_noalloc_addr[dev];
+  b.workspace_bytes = kNoAllocBytes;
+  if (nsteps == 0) return GMES_OK;
+  e = launch_batch(batch_view(b), precision, disp, nsteps, 0, s);
+  if (e != cudaSuccess) return cuda_fail(e, "launching batch kernels");
+  return GMES_OK;
+}

@@ -270,6 +270,36 @@ gmes_status gmes_batch_set_steps(const gmes_batch* b, const int32_t* steps, void
 gmes_status gmes_batch_step(const gmes_batch* b, int32_t nsteps, int32_t blocks, void* stream);
 
 /*
+ * Batch step that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory: a process whose memory
+ * pool already owns the GPU's free memory and forbids further cudaMalloc
+ * (a serving host, or a plugin inside a framework that controls
+ * allocation), and latency-sensitive loops that must not pay the implicit
+ * device synchronisation a cudaMalloc can cost.  Instead of a caller
+ * workspace, the batch tables live in one fixed array in the library's
+ * device memory, sized for at most GMES_NOALLOC_MAX_GRIDS grids; every GPU
+ * that loads the library keeps that array until the process exits.  The
+ * call rebuilds the tables for `grids` (same rules as gmes_batch_prepare),
+ * then advances grid g by steps[g] of the nsteps steps (same as
+ * gmes_batch_set_steps + gmes_batch_step), reading each grid's staged
+ * source values.
+ *   - The first call on a device also looks up that array's device address
+ *     (with the device current); make that first call before any stream
+ *     capture.
+ *   - All calls share the one array: calls that overlap on the GPU (other
+ *     streams, other threads) race and corrupt each other's tables.
+ *     Calls on one stream are ordered.
+ *   - More than GMES_NOALLOC_MAX_GRIDS grids is rejected with
+ *     GMES_ERR_VALUE.
+ *   - On success no host or device memory is allocated or freed.
+ */
+#define GMES_NOALLOC_MAX_GRIDS 64
+gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grids, const int32_t* steps,
+                                    int32_t njobs, int32_t nsteps, int32_t bx_cap,
+                                    void* stream);
+
+/*
  * CUDA graphs of whole chunks (stream capture of gmes_step / gmes_batch_step
  * on a non-default stream).  The graph bakes in the descriptors' device
  * pointers: replay it only while the same buffers are alive.
