@@ -27,6 +27,8 @@ EXPORTS = [
     "gmes_batch_workspace_size", "gmes_batch_prepare", "gmes_batch_set_steps", "gmes_batch_step",
     "gmes_graph_capture_step", "gmes_graph_capture_batch", "gmes_graph_launch",
     "gmes_graph_destroy", "gmes_rasterize", "gmes_batch_step_noalloc",
+    "gmes_tmz_sizes", "gmes_tmz_check", "gmes_tmz_set_design", "gmes_tmz_reset",
+    "gmes_tmz_forward", "gmes_tmz_objective", "gmes_tmz_adjoint",
 ]
 NOALLOC_MAX_GRIDS = 64
 
@@ -75,6 +77,18 @@ class BatchC(C.Structure):
     _fields_ = [("njobs", C.c_int32), ("precision", C.c_int32), ("dispersive", C.c_int32),
                 ("srcs", C.c_int32), ("tiles", C.c_int64), ("ghosts", C.c_int64),
                 ("workspace", C.c_void_p), ("workspace_bytes", C.c_int64)]
+
+
+TMZ_RECORD_MONITOR, TMZ_RECORD_HIST = 1, 2
+
+
+class TmzBatchC(C.Structure):
+    _fields_ = [("nbatch", C.c_int32), ("design_lo", C.c_int32 * 2), ("design_n", C.c_int32 * 2),
+                ("monitor_lo", C.c_int32 * 2), ("monitor_n", C.c_int32 * 2),
+                ("nsrc", C.c_int32), ("total_steps", C.c_int32), ("hist_steps", C.c_int32),
+                ("state", C.c_void_p), ("adjoint", C.c_void_p), ("design", C.c_void_p),
+                ("hist", C.c_void_p), ("monitor", C.c_void_p), ("grad", C.c_void_p),
+                ("weight", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p)]
 
 
 class GmesError(RuntimeError):
@@ -129,6 +143,14 @@ def load():
     lib.gmes_rasterize.argtypes = [P(GridDescC), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                    C.c_void_p]
     lib.gmes_graph_destroy.argtypes = [C.c_void_p]
+    G, B = P(GridDescC), P(TmzBatchC)
+    lib.gmes_tmz_sizes.argtypes = [G, B, P(C.c_int64)]
+    lib.gmes_tmz_check.argtypes = [G, B]
+    lib.gmes_tmz_set_design.argtypes = [G, B, C.c_void_p, C.c_void_p]
+    lib.gmes_tmz_reset.argtypes = [G, B, C.c_int32, C.c_void_p]
+    lib.gmes_tmz_forward.argtypes = [G, B, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]
+    lib.gmes_tmz_objective.argtypes = [G, B, C.c_int32, C.c_void_p, C.c_void_p]
+    lib.gmes_tmz_adjoint.argtypes = [G, B, C.c_int32, C.c_int32, C.c_void_p]
     for name in EXPORTS:
         if name not in ("gmes_abi_version", "gmes_last_error", "gmes_elem_size",
                         "gmes_batch_workspace_size"):

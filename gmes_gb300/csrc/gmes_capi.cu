@@ -624,6 +624,224 @@ gmes_status gmes_write_field(const gmes_grid_desc* g, int32_t comp, const double
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
+// Differentiation: batched TMz forward / adjoint (gmes_adjoint.cu).
+// ---------------------------------------------------------------------------
+namespace gmes {
+namespace {
+
+constexpr int32_t kTmzActive = (1 << GMES_EZ) | (1 << GMES_HX) | (1 << GMES_HY);
+
+struct TmzLayout {
+  int64_t array;  // bytes of one [nb][nx][ny] array, 256-aligned
+  int64_t state, adjoint, design, hist, monitor, grad;
+};
+
+TmzLayout tmz_layout(const gmes_grid_desc& g, const gmes_tmz_batch& b) {
+  TmzLayout L;
+  const int64_t es = elem_size(g.precision);
+  const int64_t plane = (int64_t)g.n[0] * g.n[1];
+  const int64_t nd = (int64_t)b.design_n[0] * b.design_n[1];
+  const int64_t nm = (int64_t)b.monitor_n[0] * b.monitor_n[1];
+  L.array = align256((int64_t)b.nbatch * plane * es);
+  L.state = kTmzState * L.array;
+  L.adjoint = kTmzAdjoint * L.array;
+  L.design = align256((int64_t)b.nbatch * nd * (int64_t)sizeof(DesignCoef));
+  L.hist = align256((int64_t)b.hist_steps * b.nbatch * nd * es);
+  L.monitor = align256((int64_t)b.nbatch * b.total_steps * nm * 8);
+  L.grad = align256((int64_t)b.nbatch * nd * 8);
+  return L;
+}
+
+gmes_status check_tmz(const gmes_grid_desc* g, const gmes_tmz_batch* b, bool need_buffers) {
+  gmes_status st = check_desc(g, need_buffers);
+  if (st != GMES_OK) return st;
+  if (b == nullptr) return fail(GMES_ERR_VALUE, "batch descriptor is NULL");
+  if (g->active != kTmzActive || g->n[2] != 1)
+    return fail(GMES_ERR_VALUE, "the adjoint path needs a TMz grid (Ez, Hx, Hy; n[2] = 1)");
+  if (g->precision == GMES_FP64_STRICT)
+    return fail(GMES_ERR_VALUE, "fp64_strict has no adjoint path; use fp64");
+  if (b->nbatch < 1 || b->nbatch > 65535)
+    return fail(GMES_ERR_VALUE, "nbatch = %d outside [1, 65535]", b->nbatch);
+  const int32_t nn[2] = {g->n[0], g->n[1]};
+  for (int a = 0; a < 2; ++a) {
+    if (b->design_n[a] < 1 || b->design_lo[a] < 0 || b->design_lo[a] + b->design_n[a] > nn[a])
+      return fail(GMES_ERR_INDEX, "design box outside the %d x %d lattice", nn[0], nn[1]);
+    if (b->monitor_n[a] < 1 || b->monitor_lo[a] < 0 || b->monitor_lo[a] + b->monitor_n[a] > nn[a])
+      return fail(GMES_ERR_INDEX, "monitor box outside the %d x %d lattice", nn[0], nn[1]);
+  }
+  if (b->nsrc < 0 || b->total_steps < 1 || b->hist_steps < 0)
+    return fail(GMES_ERR_VALUE, "negative nsrc / hist_steps or total_steps < 1");
+  if (need_buffers) {
+    if (!b->state || !b->adjoint || !b->design || !b->monitor || !b->grad)
+      return fail(GMES_ERR_VALUE, "a batch buffer is NULL");
+    if (b->hist_steps > 0 && !b->hist) return fail(GMES_ERR_VALUE, "hist is NULL");
+    if (b->nsrc > 0 && (!b->src || !b->src_val))
+      return fail(GMES_ERR_VALUE, "nsrc > 0 but src or src_val is NULL");
+  }
+  return GMES_OK;
+}
+
+TmzDev make_tmz_dev(const gmes_grid_desc& g, const gmes_tmz_batch& b) {
+  const TmzLayout L = tmz_layout(g, b);
+  TmzDev t;
+  std::memset(&t, 0, sizeof(t));
+  t.nx = g.n[0];
+  t.ny = g.n[1];
+  t.nb = b.nbatch;
+  t.nsrc = b.nsrc;
+  t.plane = (int64_t)g.n[0] * g.n[1];
+  for (int a = 0; a < 2; ++a) {
+    t.d0[a] = b.design_lo[a];
+    t.dn[a] = b.design_n[a];
+    t.m0[a] = b.monitor_lo[a];
+    t.mn[a] = b.monitor_n[a];
+  }
+  t.total_steps = b.total_steps;
+  t.hist_steps = b.hist_steps;
+  char* s = static_cast<char*>(b.state);
+  for (int k = 0; k < kTmzState; ++k) t.f[k] = s + k * L.array;
+  char* a = static_cast<char*>(b.adjoint);
+  for (int k = 0; k < 3; ++k) t.l[k] = a + k * L.array;
+  for (int r = 0; r < 2; ++r)
+    for (int k = 0; k < 4; ++k) t.phi[r][k] = a + (3 + 4 * r + k) * L.array;
+  t.dc = static_cast<const DesignCoef*>(b.design);
+  t.hist = b.hist;
+  t.mon = b.monitor;
+  t.grad = b.grad;
+  t.weight = b.weight;
+  t.src = b.src;
+  t.src_val = b.src_val;
+  return t;
+}
+
+}  // namespace
+}  // namespace gmes
+
+extern "C" {
+
+gmes_status gmes_tmz_sizes(const gmes_grid_desc* g, const gmes_tmz_batch* b, int64_t sizes[6]) {
+  gmes_status st = check_tmz(g, b, false);
+  if (st != GMES_OK) return st;
+  if (sizes == nullptr) return fail(GMES_ERR_VALUE, "sizes is NULL");
+  const TmzLayout L = tmz_layout(*g, *b);
+  sizes[0] = L.state;
+  sizes[1] = L.adjoint;
+  sizes[2] = L.design;
+  sizes[3] = L.hist;
+  sizes[4] = L.monitor;
+  sizes[5] = L.grad;
+  return GMES_OK;
+}
+
+gmes_status gmes_tmz_check(const gmes_grid_desc* g, const gmes_tmz_batch* b) {
+  gmes_status st = check_tmz(g, b, true);
+  if (st != GMES_OK) return st;
+  const CoefLayout CL = coef_layout(*g);
+  const char* base = static_cast<const char*>(g->coef);
+  int kinds[3][GMES_MAX_CLASSES];
+  for (int c = 2; c < 5; ++c) {
+    std::vector<ClassCoef> tab(g->nclass[c]);
+    cudaError_t e = cudaMemcpy(tab.data(), base + CL.class_tab[c],
+                               tab.size() * sizeof(ClassCoef), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "reading the class table");
+    for (int k = 0; k < GMES_MAX_CLASSES; ++k) kinds[c - 2][k] = GMES_KIND_DUMMY;
+    for (int k = 0; k < g->nclass[c]; ++k) {
+      const int kind = tab[k].kind;
+      if (kind != GMES_KIND_DUMMY && kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML)
+        return fail(GMES_ERR_VALUE,
+                    "component %d class %d has kind %d; the adjoint path supports "
+                    "DIELECTRIC, CPML and DUMMY", c, k, kind);
+      kinds[c - 2][k] = kind;
+    }
+  }
+  // the design box's Ez points must be dielectric
+  const int64_t sez1 = g->n[2];                 // Ez shape (n0+1, n1+1, 1)
+  const int64_t sez0 = (int64_t)(g->n[1] + 1) * sez1;
+  std::vector<uint8_t> ids((size_t)b->design_n[0] * b->design_n[1]);
+  cudaError_t e = cudaMemcpy2D(ids.data(), (size_t)b->design_n[1],
+                               g->cls[2] + b->design_lo[0] * sez0 + b->design_lo[1] * sez1,
+                               (size_t)sez0, (size_t)b->design_n[1], (size_t)b->design_n[0],
+                               cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "reading the Ez class map");
+  for (size_t k = 0; k < ids.size(); ++k)
+    if (kinds[0][ids[k]] != GMES_KIND_DIELECTRIC)
+      return fail(GMES_ERR_VALUE, "design point %zu is not on a dielectric Ez point", k);
+  return GMES_OK;
+}
+
+gmes_status gmes_tmz_set_design(const gmes_grid_desc* g, const gmes_tmz_batch* b,
+                                const double* eps, void* stream) {
+  gmes_status st = check_tmz(g, b, true);
+  if (st != GMES_OK) return st;
+  if (eps == nullptr) return fail(GMES_ERR_VALUE, "eps is NULL");
+  cudaError_t e = launch_tmz_design(make_grid_dev(*g), make_tmz_dev(*g, *b), eps,
+                                    static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching the design kernel");
+  return GMES_OK;
+}
+
+gmes_status gmes_tmz_reset(const gmes_grid_desc* g, const gmes_tmz_batch* b, int32_t what,
+                           void* stream) {
+  gmes_status st = check_tmz(g, b, true);
+  if (st != GMES_OK) return st;
+  const TmzLayout L = tmz_layout(*g, *b);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSuccess;
+  if (what & 1) e = cudaMemsetAsync(b->state, 0, (size_t)L.state, s);
+  if (e == cudaSuccess && (what & 2)) e = cudaMemsetAsync(b->adjoint, 0, (size_t)L.adjoint, s);
+  if (e == cudaSuccess && (what & 2))
+    e = cudaMemsetAsync(b->grad, 0, (size_t)b->nbatch * b->design_n[0] * b->design_n[1] * 8, s);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing the batch");
+  return GMES_OK;
+}
+
+gmes_status gmes_tmz_forward(const gmes_grid_desc* g, const gmes_tmz_batch* b, int32_t step0,
+                             int32_t nsteps, int32_t flags, void* stream) {
+  gmes_status st = check_tmz(g, b, true);
+  if (st != GMES_OK) return st;
+  if (step0 < 0 || nsteps < 0 || (int64_t)step0 + nsteps > b->total_steps)
+    return fail(GMES_ERR_INDEX, "steps %d..%d outside 1..%d", step0 + 1, step0 + nsteps,
+                b->total_steps);
+  if ((flags & ~3) != 0) return fail(GMES_ERR_VALUE, "unknown flags 0x%x", flags);
+  if ((flags & GMES_TMZ_RECORD_HIST) && nsteps > b->hist_steps)
+    return fail(GMES_ERR_VALUE, "%d steps exceed the hist capacity %d", nsteps, b->hist_steps);
+  cudaError_t e = launch_tmz_forward(g->precision, make_grid_dev(*g), make_tmz_dev(*g, *b),
+                                     step0, nsteps, flags, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching the forward kernels");
+  return GMES_OK;
+}
+
+gmes_status gmes_tmz_objective(const gmes_grid_desc* g, const gmes_tmz_batch* b,
+                               int32_t nsteps, double* J, void* stream) {
+  gmes_status st = check_tmz(g, b, true);
+  if (st != GMES_OK) return st;
+  if (J == nullptr) return fail(GMES_ERR_VALUE, "J is NULL");
+  if (nsteps < 0 || nsteps > b->total_steps)
+    return fail(GMES_ERR_INDEX, "nsteps = %d outside [0, %d]", nsteps, b->total_steps);
+  cudaError_t e = launch_tmz_objective(make_grid_dev(*g), make_tmz_dev(*g, *b), nsteps, J,
+                                       static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching the objective kernel");
+  return GMES_OK;
+}
+
+gmes_status gmes_tmz_adjoint(const gmes_grid_desc* g, const gmes_tmz_batch* b, int32_t step0,
+                             int32_t nsteps, void* stream) {
+  gmes_status st = check_tmz(g, b, true);
+  if (st != GMES_OK) return st;
+  if (step0 < 0 || nsteps < 0 || (int64_t)step0 + nsteps > b->total_steps)
+    return fail(GMES_ERR_INDEX, "steps %d..%d outside 1..%d", step0 + 1, step0 + nsteps,
+                b->total_steps);
+  if (nsteps > b->hist_steps)
+    return fail(GMES_ERR_VALUE, "%d steps exceed the hist capacity %d", nsteps, b->hist_steps);
+  cudaError_t e = launch_tmz_adjoint(g->precision, make_grid_dev(*g), make_tmz_dev(*g, *b),
+                                     step0, nsteps, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching the adjoint kernels");
+  return GMES_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
 // gmes_batch_step_noalloc: the batch tables in a fixed device array.
 // ---------------------------------------------------------------------------
 namespace gmes {

@@ -258,6 +258,48 @@ struct BatchView {
   int64_t ghosts;
 };
 
+// ---------------------------------------------------------------------------
+// Differentiation (batched TMz forward + adjoint, gmes_adjoint.cu).
+// ---------------------------------------------------------------------------
+// Per design pixel: the Ez update coefficients dt/eps/dx, dt/eps/dy (built
+// like a dielectric class's c1, c2) and -1/eps for the gradient.
+struct DesignCoef {
+  Coef c1, c2;
+  double neg_reps;
+  double eps;
+};
+
+// Number of arrays in the forward state and adjoint blocks.
+constexpr int kTmzState = 7;    // Ez, Hx, Hy, psi_ez(x), psi_ez(y), psi_hx(y), psi_hy(x)
+constexpr int kTmzAdjoint = 11; // lambda Ez, Hx, Hy, then 2 x the adjoints of the 4 psi
+
+struct TmzDev {
+  int32_t nx, ny, nb, nsrc;
+  int64_t plane;            // nx * ny lattice points per array per design
+  int32_t d0[2], dn[2];     // design box (lattice indices, extent)
+  int32_t m0[2], mn[2];     // monitor box
+  int32_t total_steps, hist_steps;
+  void* f[kTmzState];       // [nb][nx][ny] each
+  void* l[3];
+  void* phi[2][4];          // ping-pong buffers of the psi adjoints
+  const DesignCoef* dc;     // [nb][nd]
+  void* hist;               // [hist_steps][nb][nd]
+  double* mon;              // [nb][total_steps][nm]
+  double* grad;             // [nb][nd]
+  const double* weight;     // [nb] or null
+  const gmes_point_source* src;
+  const double* src_val;    // [total_steps][2][nsrc]
+};
+
+cudaError_t launch_tmz_design(const GridDev& g, const TmzDev& t, const double* eps,
+                              cudaStream_t s);
+cudaError_t launch_tmz_forward(int precision, const GridDev& g, const TmzDev& t, int step0,
+                               int nsteps, int flags, cudaStream_t s);
+cudaError_t launch_tmz_adjoint(int precision, const GridDev& g, const TmzDev& t, int step0,
+                               int nsteps, cudaStream_t s);
+cudaError_t launch_tmz_objective(const GridDev& g, const TmzDev& t, int nsteps, double* J,
+                                 cudaStream_t s);
+
 // Host-side helpers implemented in gmes_capi.cu.
 GridDev make_grid_dev(const gmes_grid_desc& g);
 

@@ -13,12 +13,17 @@ distributions of the benchmark configurations:
                 Drude spheres (omega_p 9, gamma 0.07, radius 10-20 cells), a
                 Lorentz slab (2.0, 3.0, 0.1), a DCP-ADE sphere (1 Drude term +
                 2 seeded critical points), 12-cell UPML, 2000 steps.
+* ``design2d``  2-D TMz N^2 (default 512^2) differentiation scene: vacuum,
+                20-cell CPML, an Ez-polarised line source (a column of Jz
+                point sources, Bandpass(0.5, 0.5)) left of a 64x64-point
+                design region, an 8x8 monitor patch right of it, 2000 steps,
+                a batch of seeded designs with eps uniform in [1, 12].
 """
 
 import numpy as np
 
 from . import (Bandpass, Block, Cartesian, Continuous, Cpml, CriticalPoint, DcpAde,
-               DefaultMedium, Dielectric, Drude, DrudePole, Ex, Ez, FDTD, Lorentz,
+               DefaultMedium, Dielectric, Drude, DrudePole, Ex, Ez, FDTD, Jz, Lorentz,
                LorentzPole, PointSource, Shell, Sphere, TMzFDTD, Upml)
 
 
@@ -170,3 +175,34 @@ def _serving_builder(side, three_d, pml, kind, eps, precision):
         space = Cartesian(size=(size, size, 0), resolution=res)
         return TMzFDTD(space, geom, src, verbose=False, precision=precision)
     return build
+
+
+def design2d(n=512, res=20, pml_cells=20, design_px=64, monitor_px=8, nsteps=2000, batch=64,
+             seed=0, hard=False, src_time=None, background=None):
+    """The differentiation scene: returns (space, geom_list, src_list, design, monitor, eps, nsteps).
+
+    The source column sits a quarter of the interior left of the centre,
+    the design region is centred, the monitor patch a quarter right.
+    ``hard`` uses hard Ez point sources instead of Jz current sources;
+    ``background`` adds dielectric blocks (list of (center, size, eps)).
+    ``eps`` is (batch, design_px, design_px) float64, uniform in [1, 12].
+    """
+    from .adjoint import DesignRegion
+    dx = 1.0 / res
+    size = n * dx
+    inner = size / 2 - pml_cells * dx
+    geom = [DefaultMedium(material=Dielectric())]
+    for center, bsize, eps in background or []:
+        geom.append(Block(material=Dielectric(eps_inf=eps), center=center, size=bsize))
+    geom.append(Shell(material=Cpml(), thickness=pml_cells * dx))
+    st = src_time or Bandpass(freq=0.5, fwidth=0.5)
+    x_src = -inner / 2
+    ny_src = int(round(2 * inner / dx)) - 1
+    src = [PointSource(src_time=st, center=(x_src, -inner + (q + 1) * dx, 0),
+                       component=Ez if hard else Jz) for q in range(ny_src)]
+    space = Cartesian(size=(size, size, 0), resolution=res)
+    design = DesignRegion(center=(0.0, 0.0), size=(design_px * dx, design_px * dx))
+    monitor = DesignRegion(center=(inner / 2, 0.0), size=(monitor_px * dx, monitor_px * dx))
+    rng = np.random.default_rng(seed)
+    eps = rng.uniform(1.0, 12.0, (batch, design_px, design_px))
+    return space, geom, src, design, monitor, eps, nsteps

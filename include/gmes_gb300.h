@@ -350,6 +350,72 @@ gmes_status gmes_read_field(const gmes_grid_desc* g, int32_t comp, double* host_
 gmes_status gmes_write_field(const gmes_grid_desc* g, int32_t comp, const double* host_in,
                              void* stream);
 
+/*
+ * Differentiation (no counterpart in the reference, which has no adjoint).
+ *
+ * A batch of TMz designs shares one grid (geometry, CPML, sources: a
+ * gmes_grid_desc with active = Ez|Hx|Hy, n[2] = 1, built as usual) and
+ * differs only in the permittivity of a rectangular design box of Ez
+ * points.  The forward kernels advance the batch and record the Ez values
+ * of a monitor box after every step; gmes_tmz_objective gives
+ *     J_b = dt * sum_{n=1..N} sum_{monitor} Ez_n^2;
+ * gmes_tmz_adjoint runs the time-reversed (transposed) step and
+ * accumulates dJ_b/deps into grad.  Steps are numbered 1..total_steps;
+ * step n takes the state after n-1 steps to the state after n steps.
+ *
+ * Fields live on a periodic nx x ny lattice per design, without the
+ * reference's ghost planes: Ez[i,j,0], Hx[i,j+1,1], Hy[i+1,j,1] of the grid
+ * arrays are lattice point (i, j) of arrays 0, 1, 2.  Supported classes
+ * of Ez, Hx, Hy: DIELECTRIC, CPML, DUMMY (gmes_tmz_check rejects others);
+ * the design box must lie on DIELECTRIC Ez points.
+ */
+#define GMES_TMZ_RECORD_MONITOR 1 /* forward: write the monitor rows of these steps */
+#define GMES_TMZ_RECORD_HIST 2    /* forward: write the design increments (slot = step - step0 - 1) */
+
+typedef struct {
+  int32_t nbatch;        /* designs */
+  int32_t design_lo[2];  /* lattice (i, j) of the design box's first point */
+  int32_t design_n[2];   /* design box extent */
+  int32_t monitor_lo[2];
+  int32_t monitor_n[2];
+  int32_t nsrc;          /* point sources: comp 2 (Ez), 3 (Hx), 4 (Hy); offset = i * ny + j */
+  int32_t total_steps;   /* rows of monitor and src_val */
+  int32_t hist_steps;    /* capacity of hist in steps (one checkpoint segment) */
+  /* device buffers (sizes from gmes_tmz_sizes) */
+  void* state;           /* 7 arrays [nbatch][nx][ny]: Ez, Hx, Hy and the 4 CPML psi */
+  void* adjoint;         /* 11 arrays: adjoints of Ez, Hx, Hy and 2 x 4 psi adjoints */
+  void* design;          /* per-pixel coefficients, written by gmes_tmz_set_design */
+  void* hist;            /* [hist_steps][nbatch][design points] Ez increments */
+  double* monitor;       /* [nbatch][total_steps][monitor points] */
+  double* grad;          /* [nbatch][design points] dJ_b / deps */
+  const double* weight;  /* [nbatch] seed scale of each J_b (dL/dJ_b), or NULL for 1 */
+  const gmes_point_source* src;
+  const double* src_val; /* [total_steps][2][nsrc]: E-half and H-half values */
+} gmes_tmz_batch;
+
+/* Bytes of state, adjoint, design, hist, monitor, grad. */
+gmes_status gmes_tmz_sizes(const gmes_grid_desc* g, const gmes_tmz_batch* b, int64_t sizes[6]);
+/* Validate the classes of Ez/Hx/Hy and the design box against the grid's
+   coefficient block and class maps (synchronous: copies them to the host). */
+gmes_status gmes_tmz_check(const gmes_grid_desc* g, const gmes_tmz_batch* b);
+/* Design coefficients from eps (device, [nbatch][design points], > 0). */
+gmes_status gmes_tmz_set_design(const gmes_grid_desc* g, const gmes_tmz_batch* b,
+                                const double* eps, void* stream);
+/* Zero the state (what & 1) and/or the adjoint and grad (what & 2). */
+gmes_status gmes_tmz_reset(const gmes_grid_desc* g, const gmes_tmz_batch* b, int32_t what,
+                           void* stream);
+/* Steps step0+1 .. step0+nsteps forward; flags GMES_TMZ_RECORD_*. */
+gmes_status gmes_tmz_forward(const gmes_grid_desc* g, const gmes_tmz_batch* b, int32_t step0,
+                             int32_t nsteps, int32_t flags, void* stream);
+/* J[b] (device, nbatch doubles) from the first nsteps monitor rows. */
+gmes_status gmes_tmz_objective(const gmes_grid_desc* g, const gmes_tmz_batch* b,
+                               int32_t nsteps, double* J, void* stream);
+/* Steps step0+nsteps down to step0+1 backward, seeding each with its
+   monitor row; needs the hist of the same steps (a forward call with
+   GMES_TMZ_RECORD_HIST from the state after step0). */
+gmes_status gmes_tmz_adjoint(const gmes_grid_desc* g, const gmes_tmz_batch* b, int32_t step0,
+                             int32_t nsteps, void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* gmes_last_error(void);
 

@@ -608,6 +608,248 @@ int oracle_step(oracle* o, int nsteps, const double* src_vals) {
   return 0;
 }
 
+/* ---- reset and per-point permittivity ------------------------------------ */
+
+/* Zero every field and every per-point state (psi, d, ADE). */
+int oracle_reset(oracle* o) {
+  for (int c = 0; c < 6; ++c) {
+    memset(o->f[c], 0, sizeof(double) * (size_t)(o->sh[c][0] * o->sh[c][1] * o->sh[c][2]));
+    for (int k = 0; k < o->nupd[c]; ++k) {
+      updater* u = &o->upd[c][k];
+      for (int64_t t = 0; t < u->count; ++t) {
+        if (u->kind == K_CPML) { ((p_cpml*)u->pts)[t].psi1 = 0; ((p_cpml*)u->pts)[t].psi2 = 0; }
+        else if (u->kind == K_UPML) ((p_upml*)u->pts)[t].d = 0;
+        else if (u->kind == K_DRUDE || u->kind == K_LORENTZ || u->kind == K_DCP)
+          memset(((p_ade*)u->pts)[t].st, 0, sizeof(((p_ade*)u->pts)[t].st));
+      }
+    }
+  }
+  return 0;
+}
+
+/* Give the dielectric points at offsets off[0..n) of component c their own
+   permittivity (the reference keeps eps per point in DielectricElectricParam,
+   src/pw_dielectric.hh:18-30).  Returns -1 if an offset is not a dielectric
+   point of c. */
+int oracle_set_eps(oracle* o, int c, int n, const int64_t* off, const double* eps) {
+  for (int q = 0; q < n; ++q) {
+    int found = 0;
+    for (int k = 0; k < o->nupd[c] && !found; ++k) {
+      updater* u = &o->upd[c][k];
+      if (u->kind != K_DIEL) continue;
+      p_diel* pts = (p_diel*)u->pts;
+      for (int64_t t = 0; t < u->count; ++t)
+        if (pts[t].off == off[q]) { pts[t].eps = eps[q]; found = 1; break; }
+    }
+    if (!found) return -1;
+  }
+  return 0;
+}
+
+/* ---- discrete adjoint (test infrastructure; the reference has none) ------- *
+ * J = dt * sum_{n=1..N} sum_m F_{c_m}[off_m]^2 after each step n.  The
+ * backward sweep applies the transpose of every operation of oracle_step in
+ * reverse order, in scatter form on the full arrays: H sources, H updaters,
+ * the E ghost-plane copies (plane by plane, last copy first), E sources,
+ * E updaters (with the gradient of the design points), the H ghost copies.
+ * Supported classes: Dielectric, CPML (and Dummy).  Serial. */
+#define LAT(L, c, i, j, k) (L[c][((int64_t)(i) * o->sh[c][1] + (j)) * o->sh[c][2] + (k)])
+
+static void scatter_diffs(const oracle* o, double** L, int c, const int x[3], double w1,
+                          double w2) {
+  const int own = c % 3, a1 = (own + 1) % 3, a2 = (own + 2) % 3;
+  if (c < 3) {
+    const int in1 = 3 + a2, in2 = 3 + a1;
+    int p[3] = {x[0], x[1], x[2]}, q[3];
+    p[own] += 1;
+    if (o->active & (1 << in1)) {
+      memcpy(q, p, sizeof(q)); q[a1] += 1;
+      LAT(L, in1, q[0], q[1], q[2]) += w1;
+      LAT(L, in1, p[0], p[1], p[2]) -= w1;
+    }
+    if (o->active & (1 << in2)) {
+      memcpy(q, p, sizeof(q)); q[a2] += 1;
+      LAT(L, in2, q[0], q[1], q[2]) += w2;
+      LAT(L, in2, p[0], p[1], p[2]) -= w2;
+    }
+  } else {
+    const int in1 = a2, in2 = a1;
+    if (o->active & (1 << in1)) {
+      int u[3] = {x[0], x[1], x[2]}; u[a2] -= 1;
+      int v[3] = {u[0], u[1], u[2]}; v[a1] -= 1;
+      LAT(L, in1, u[0], u[1], u[2]) += w1;
+      LAT(L, in1, v[0], v[1], v[2]) -= w1;
+    }
+    if (o->active & (1 << in2)) {
+      int u[3] = {x[0], x[1], x[2]}; u[a1] -= 1;
+      int v[3] = {u[0], u[1], u[2]}; v[a2] -= 1;
+      LAT(L, in2, u[0], u[1], u[2]) += w2;
+      LAT(L, in2, v[0], v[1], v[2]) -= w2;
+    }
+  }
+}
+
+/* Transpose of one updater; lpsi holds 2 psi adjoints per CPML point. */
+static void adjoint_updater(const oracle* o, double** L, const updater* u, double* lpsi) {
+  const int c = u->comp;
+  const int own = c % 3, a1 = (own + 1) % 3, a2 = (own + 2) % 3;
+  const double d1 = o->dr[a1], d2 = o->dr[a2], dt = o->dt;
+  const int E = c < 3;
+  if (u->kind == K_DIEL) {
+    const p_diel* pts = (const p_diel*)u->pts;
+    for (int64_t t = 0; t < u->count; ++t) {
+      const double lf = L[c][pts[t].off];
+      const double s = dt / pts[t].eps;
+      if (E)
+        scatter_diffs(o, L, c, pts[t].idx, s / d1 * lf, -s / d2 * lf);
+      else
+        scatter_diffs(o, L, c, pts[t].idx, -s / d1 * lf, s / d2 * lf);
+    }
+  } else if (u->kind == K_CPML) {
+    const p_cpml* pts = (const p_cpml*)u->pts;
+    for (int64_t t = 0; t < u->count; ++t) {
+      const p_cpml* p = &pts[t];
+      const double lf = L[c][p->off];
+      const double s = E ? dt / p->eps : -dt / p->eps;
+      const double L1 = lpsi[2 * t] + s * lf;
+      const double L2 = lpsi[2 * t + 1] - s * lf;
+      const double w1 = p->c1 / d1 * L1 + s / (d1 * p->k1) * lf;
+      const double w2 = p->c2 / d2 * L2 - s / (d2 * p->k2) * lf;
+      lpsi[2 * t] = p->b1 * L1;
+      lpsi[2 * t + 1] = p->b2 * L2;
+      scatter_diffs(o, L, c, p->idx, w1, w2);
+    }
+  }
+}
+
+static void adjoint_copy_plane(const oracle* o, double** L, int c, int axis, int64_t dst,
+                               int64_t src) {
+  const int64_t* sh = o->sh[c];
+  const int p = (axis + 1) % 3, q = (axis + 2) % 3;
+  for (int64_t a = 0; a < sh[p]; ++a)
+    for (int64_t b = 0; b < sh[q]; ++b) {
+      int64_t x[3], y[3];
+      x[axis] = dst; x[p] = a; x[q] = b;
+      y[axis] = src; y[p] = a; y[q] = b;
+      const double v = LAT(L, c, x[0], x[1], x[2]);
+      LAT(L, c, x[0], x[1], x[2]) = 0;
+      LAT(L, c, y[0], y[1], y[2]) += v;
+    }
+}
+
+static void adjoint_chatter(const oracle* o, double** L, int c) {
+  if (!(o->active & (1 << c))) return;
+  const int own = c % 3;
+  const int ax[2] = {(own + 1) % 3, (own + 2) % 3};
+  for (int h = 1; h >= 0; --h) {
+    const int64_t last = o->sh[c][ax[h]] - 1;
+    if (c < 3)
+      adjoint_copy_plane(o, L, c, ax[h], last, 0);
+    else
+      adjoint_copy_plane(o, L, c, ax[h], 0, last);
+  }
+}
+
+static void adjoint_sources(const oracle* o, double** L, int side) {
+  for (int q = 0; q < o->nsrc; ++q) {
+    const int c = o->src_comp[q];
+    if ((c < 3) != (side == 0) || o->src_mode[q] != 0) continue;
+    L[c][o->src_off[q]] = 0;
+  }
+}
+
+static const p_diel* find_diel(const oracle* o, int c, int64_t off) {
+  for (int k = 0; k < o->nupd[c]; ++k) {
+    const updater* u = &o->upd[c][k];
+    if (u->kind != K_DIEL) continue;
+    const p_diel* pts = (const p_diel*)u->pts;
+    for (int64_t t = 0; t < u->count; ++t)
+      if (pts[t].off == off) return &pts[t];
+  }
+  return NULL;
+}
+
+/* Runs nsteps forward from the current state, recording the monitor and
+   the design points' curls, then (grad != NULL) the backward sweep.
+   Returns 0, -1 for an unsupported class, -2 for a design point that is not
+   a dielectric E point, -3 on allocation failure. */
+int oracle_adjoint(oracle* o, int nsteps, const double* src_vals, int nmon, const int* mcomp,
+                   const int64_t* moff, int ndes, const int* dcomp, const int64_t* doff,
+                   double* J, double* grad) {
+  for (int c = 0; c < 6; ++c)
+    for (int k = 0; k < o->nupd[c]; ++k)
+      if (o->upd[c][k].kind != K_DIEL && o->upd[c][k].kind != K_CPML) return -1;
+  const p_diel** dp = (const p_diel**)calloc((size_t)(ndes ? ndes : 1), sizeof(p_diel*));
+  double* mon = (double*)calloc((size_t)nsteps * (nmon ? nmon : 1), sizeof(double));
+  double* curl = (double*)calloc((size_t)nsteps * (ndes ? ndes : 1), sizeof(double));
+  if (!dp || !mon || !curl) { free(dp); free(mon); free(curl); return -3; }
+  for (int q = 0; q < ndes; ++q) {
+    dp[q] = dcomp[q] < 3 ? find_diel(o, dcomp[q], doff[q]) : NULL;
+    if (!dp[q]) { free(dp); free(mon); free(curl); return -2; }
+  }
+  double acc = 0;
+  for (int s = 0; s < nsteps; ++s) {
+    for (int c = 3; c < 6; ++c) chatter(o, c);
+    for (int q = 0; q < ndes; ++q) {
+      const int c = dcomp[q], own = c % 3;
+      double D1, D2;
+      diffs(o, c, dp[q]->idx, &D1, &D2);
+      curl[(int64_t)s * ndes + q] = D1 / o->dr[(own + 1) % 3] - D2 / o->dr[(own + 2) % 3];
+    }
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < o->nupd[c]; ++k) run_updater(o, &o->upd[c][k]);
+    apply_sources(o, 0, src_vals + (int64_t)(2 * s) * o->nsrc);
+    for (int c = 0; c < 3; ++c) chatter(o, c);
+    for (int c = 3; c < 6; ++c)
+      for (int k = 0; k < o->nupd[c]; ++k) run_updater(o, &o->upd[c][k]);
+    apply_sources(o, 1, src_vals + (int64_t)(2 * s + 1) * o->nsrc);
+    double js = 0;
+    for (int m = 0; m < nmon; ++m) {
+      const double v = o->f[mcomp[m]][moff[m]];
+      mon[(int64_t)s * nmon + m] = v;
+      js += v * v;
+    }
+    acc += js;
+  }
+  *J = o->dt * acc;
+  if (grad == NULL) { free(dp); free(mon); free(curl); return 0; }
+
+  double* L[6];
+  double* lpsi[6][MAXCLS];
+  int fail = 0;
+  memset(lpsi, 0, sizeof(lpsi));
+  for (int c = 0; c < 6; ++c) {
+    L[c] = (double*)calloc((size_t)(o->sh[c][0] * o->sh[c][1] * o->sh[c][2]), sizeof(double));
+    if (!L[c]) fail = 1;
+    for (int k = 0; k < o->nupd[c]; ++k) {
+      lpsi[c][k] = (double*)calloc((size_t)(2 * o->upd[c][k].count + 1), sizeof(double));
+      if (!lpsi[c][k]) fail = 1;
+    }
+  }
+  for (int q = 0; q < ndes; ++q) grad[q] = 0;
+  for (int s = nsteps - 1; s >= 0 && !fail; --s) {
+    for (int m = 0; m < nmon; ++m) L[mcomp[m]][moff[m]] += 2 * o->dt * mon[(int64_t)s * nmon + m];
+    adjoint_sources(o, L, 1);
+    for (int c = 3; c < 6; ++c)
+      for (int k = 0; k < o->nupd[c]; ++k) adjoint_updater(o, L, &o->upd[c][k], lpsi[c][k]);
+    for (int c = 2; c >= 0; --c) adjoint_chatter(o, L, c);
+    adjoint_sources(o, L, 0);
+    for (int q = 0; q < ndes; ++q) {
+      const double eps = dp[q]->eps;
+      grad[q] += L[dcomp[q]][doff[q]] * (-o->dt / (eps * eps)) * curl[(int64_t)s * ndes + q];
+    }
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < o->nupd[c]; ++k) adjoint_updater(o, L, &o->upd[c][k], lpsi[c][k]);
+    for (int c = 5; c >= 3; --c) adjoint_chatter(o, L, c);
+  }
+  for (int c = 0; c < 6; ++c) {
+    free(L[c]);
+    for (int k = 0; k < o->nupd[c]; ++k) free(lpsi[c][k]);
+  }
+  free(dp); free(mon); free(curl);
+  return fail ? -3 : 0;
+}
+
 int oracle_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -64,6 +64,14 @@ def load():
     lib.oracle_step.restype = C.c_int
     lib.oracle_step.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
     lib.oracle_threads.restype = C.c_int
+    lib.oracle_reset.restype = C.c_int
+    lib.oracle_reset.argtypes = [C.c_void_p]
+    lib.oracle_set_eps.restype = C.c_int
+    lib.oracle_set_eps.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_int64), P(C.c_double)]
+    lib.oracle_adjoint.restype = C.c_int
+    lib.oracle_adjoint.argtypes = [C.c_void_p, C.c_int, P(C.c_double), C.c_int, P(C.c_int),
+                                   P(C.c_int64), C.c_int, P(C.c_int), P(C.c_int64),
+                                   P(C.c_double), P(C.c_double)]
     lib.oracle_destroy.argtypes = [C.c_void_p]
     _lib = lib
     return lib
@@ -146,6 +154,56 @@ class Oracle:
         if self.lib.oracle_pml_profile(self.h, pml, c, axis, _dp(out)) != 0:
             raise IndexError("bad pml index")
         return out
+
+    def reset(self):
+        """Zero the fields and every per-point state; time returns to 0."""
+        self.lib.oracle_reset(self.h)
+        self.n = 0.0
+
+    def set_eps(self, c, points, eps):
+        """Per-point permittivity of dielectric points (c, index tuples) of component c."""
+        sh = self.scene.shape(c)
+        off = np.ascontiguousarray([np.ravel_multi_index(tuple(p), sh) for p in points],
+                                   np.int64)
+        e = np.ascontiguousarray(eps, np.float64).reshape(-1)
+        if self.lib.oracle_set_eps(self.h, c, len(off), off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                   _dp(e)) != 0:
+            raise ValueError("a point is not a dielectric point of this component")
+
+    def adjoint(self, nsteps, monitor, design, gradient=True):
+        """(J, dJ/deps) of J = dt * sum_n sum_monitor F^2 over nsteps steps from the current state.
+
+        ``monitor`` and ``design``: lists of (component, index tuple); the
+        gradient is with respect to the permittivity of each design point.
+        """
+        from gmes_gb300.scene import source_values
+        vals = np.ascontiguousarray(source_values(self.scene, self.scene.dt, self.n, nsteps))
+        if vals.size == 0:
+            vals = np.zeros(1)
+
+        def flat(pts):
+            comp = np.ascontiguousarray([c for c, _ in pts], np.int32)
+            off = np.ascontiguousarray(
+                [np.ravel_multi_index(tuple(i), self.scene.shape(c)) for c, i in pts], np.int64)
+            return comp, off
+
+        mc, mo = flat(monitor)
+        dc, do = flat(design)
+        J = C.c_double()
+        grad = np.zeros(max(1, len(design)), np.float64)
+        r = self.lib.oracle_adjoint(
+            self.h, int(nsteps), _dp(vals), len(mc), mc.ctypes.data_as(C.POINTER(C.c_int)),
+            mo.ctypes.data_as(C.POINTER(C.c_int64)), len(dc),
+            dc.ctypes.data_as(C.POINTER(C.c_int)), do.ctypes.data_as(C.POINTER(C.c_int64)),
+            C.byref(J), _dp(grad) if gradient else None)
+        if r == -1:
+            raise ValueError("the adjoint supports Dielectric and CPML classes only")
+        if r == -2:
+            raise ValueError("a design point is not a dielectric E point")
+        if r != 0:
+            raise MemoryError("oracle adjoint allocation failed")
+        self.n += nsteps
+        return J.value, grad[:len(design)]
 
     @staticmethod
     def threads():

@@ -105,3 +105,35 @@ def test_step_rejects_null_buffers_without_touching_the_gpu():
     d = _desc()
     with pytest.raises(ValueError, match="NULL"):
         N.check(lib.gmes_step(C.byref(d), 1, None))
+
+
+def _tmz(**kw):
+    b = N.TmzBatchC()
+    b.nbatch = kw.get("nbatch", 2)
+    lo, n = kw.get("design", ((2, 3), (4, 5)))
+    for a in range(2):
+        b.design_lo[a], b.design_n[a] = lo[a], n[a]
+        b.monitor_lo[a], b.monitor_n[a] = 1, 2
+    b.nsrc = 0
+    b.total_steps = 10
+    b.hist_steps = 4
+    return b
+
+
+def test_tmz_sizes_and_validation():
+    lib = N.load()
+    d = _desc(n=(16, 12, 1), active=(1 << 2) | (1 << 3) | (1 << 4))
+    sizes = (C.c_int64 * 6)()
+    N.check(lib.gmes_tmz_sizes(C.byref(d), C.byref(_tmz()), sizes))
+    arr = ((2 * 16 * 12 * 8 + 255) // 256) * 256
+    assert sizes[0] == 7 * arr and sizes[1] == 11 * arr
+    assert sizes[2] == ((2 * 20 * 48 + 255) // 256) * 256   # DesignCoef = 48 bytes
+    assert sizes[3] == ((4 * 2 * 20 * 8 + 255) // 256) * 256
+    assert sizes[4] == ((2 * 10 * 4 * 8 + 255) // 256) * 256
+    with pytest.raises(IndexError):
+        N.check(lib.gmes_tmz_sizes(C.byref(d), C.byref(_tmz(design=((14, 3), (4, 5)))), sizes))
+    with pytest.raises(ValueError):
+        N.check(lib.gmes_tmz_sizes(C.byref(_desc(n=(16, 12, 1))), C.byref(_tmz()), sizes))
+    d.precision = N.FP64_STRICT
+    with pytest.raises(ValueError):
+        N.check(lib.gmes_tmz_sizes(C.byref(d), C.byref(_tmz()), sizes))
