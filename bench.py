@@ -45,8 +45,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--workload", choices=("cube", "dispersive", "air2d", "serving"),
+    ap.add_argument("--workload", choices=("cube", "dispersive", "air2d", "serving", "design2d"),
                     default="cube")
+    ap.add_argument("--batch", type=int, default=64, help="design2d: designs per gradient call")
     ap.add_argument("--jobs", type=int, default=64, help="serving: number of jobs")
     ap.add_argument("--rate", type=float, default=0.0,
                     help="serving: Poisson arrival rate in jobs/s (0: all at t = 0)")
@@ -462,12 +463,110 @@ def run_serving(args):
     print(json.dumps(result), flush=True)
 
 
+def run_design(args):
+    """Gradient of the monitor objective for a batch of TMz designs (512^2, 2000 steps).
+
+    One benchmark step = one forward (J of every design, with checkpoints)
+    plus one backward (recompute + adjoint, dJ/deps of every design).
+    value = cell-updates per second counting forward, recomputed and adjoint
+    steps (3 x cells x steps x designs per benchmark step).
+    """
+    import torch
+    from gmes_gb300 import workloads as W
+    from gmes_gb300.adjoint import TMzAdjoint
+    precision = args.precision if args.precision != "fp64_strict" else "fp64"
+    n = args.n or 512
+    space, geom, src, design, monitor, eps, nsteps = W.design2d(n=n, batch=args.batch)
+    prob = TMzAdjoint(space, geom, src, design, monitor, nsteps, batch=args.batch,
+                      precision=precision)
+    cells = n * n
+    x = torch.tensor(eps, dtype=torch.float64, device="cuda")
+    for _ in range(max(1, args.warmup)):
+        prob.forward(x)
+        prob.backward()
+    torch.cuda.synchronize()
+    st = prob.grid.torch_stream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    t_fwd, t_bwd = [], []
+    clk = ClockSampler(0)
+    clk.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ev[0].record(st)
+        prob.forward(x)
+        ev[1].record(st)
+        g = prob.backward()
+        ev[2].record(st)
+        torch.cuda.synchronize()
+        t_fwd.append(ev[0].elapsed_time(ev[1]) / 1e3)
+        t_bwd.append(ev[1].elapsed_time(ev[2]) / 1e3)
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    tf, tb = statistics.median(t_fwd), statistics.median(t_bwd)
+    per = tf + tb
+    upd = 3 * cells * nsteps * args.batch
+    es = 4 if precision == "fp32" else 8
+    # algorithmic bytes per cell-step: E half reads Ez, Hx, Hy and writes Ez;
+    # H half reads Ez, Hx, Hy and writes Hx, Hy (the adjoint halves the same
+    # on the adjoint fields): 9 values.  CPML psi and the class maps (shared
+    # by the batch, L2-resident) are not counted.
+    fwd_gbs = 9 * es * cells * nsteps * args.batch / tf / 1e9
+    bwd_gbs = 2 * 9 * es * cells * nsteps * args.batch / tb / 1e9
+    peak = measured_peak()
+    result = {
+        "metric": METRIC, "value": round(upd / per / 1e9, 4), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": round(per * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp32": "f32", "df64": "df64 (f32 pair)"}[precision],
+        "data": "synthetic (seeded designs)",
+        "config": {"workload": f"design2d_tmz_{n}x{n}_adjoint", "grid": [n, n, 1],
+                   "design_points": [64, 64], "monitor_points": [8, 8], "time_steps": nsteps,
+                   "batch": args.batch, "checkpoint_segment": prob.segment,
+                   "checkpoints": (nsteps + prob.segment - 1) // prob.segment,
+                   "precision": precision,
+                   "l2": "state 7 x batch x n^2 x elem > L2 for batch 64 (inputs larger than L2)"},
+        "gradients_per_s": round(args.batch / per, 3),
+        "forward_s": round(tf, 4), "backward_s": round(tb, 4),
+        "forward_alg_GBps": round(fwd_gbs, 1), "backward_alg_GBps": round(bwd_gbs, 1),
+        "hbm_peak_GBps": peak[0] if peak else None,
+        "wall_s": round(wall, 3), "grad_finite": bool(torch.isfinite(g).all()),
+        "clocks": clocks,
+        # forward: 4 launches per step (E, E sources, H, H sources); backward:
+        # the recompute (4 per step) and the adjoint (4 per step); + design
+        # and objective
+        "gpu_launches": args.steps * (12 * nsteps + 2),
+    }
+    if not args.no_cpu_baseline:
+        result["cpu_baseline"] = design_cpu_baseline(space, geom, src, design, monitor, eps,
+                                                     prob, n)
+    print(json.dumps(result), flush=True)
+
+
+def design_cpu_baseline(space, geom, src, design, monitor, eps, prob, n, steps=100):
+    """The oracle's FP64 CPU adjoint (serial) on one design, first ``steps`` steps."""
+    from oracle.oracle import Oracle
+    (d0, dn), (m0, mn) = prob.design_box, prob.monitor_box
+    dpts = [(2, (d0[0] + a, d0[1] + b, 0)) for a in range(dn[0]) for b in range(dn[1])]
+    mpts = [(2, (m0[0] + a, m0[1] + b, 0)) for a in range(mn[0]) for b in range(mn[1])]
+    o = Oracle(prob.scene)
+    o.set_eps(2, [p for _, p in dpts], eps[0].reshape(-1))
+    t0 = time.perf_counter()
+    o.adjoint(steps, mpts, dpts)
+    dt = time.perf_counter() - t0
+    return {"value": round(2 * n * n * steps / dt / 1e9, 5), "unit": UNIT, "cores": 1,
+            "kind": "port",
+            "sample": f"oracle FP64 forward + adjoint sweep of 1 design, {steps} steps of "
+                      f"{n}x{n} (counts forward + adjoint steps)"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "serving":
         run_serving(args)
+    elif args.workload == "design2d":
+        run_design(args)
     else:
         run_ours(args)
 
