@@ -10,7 +10,7 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libgmes_gb300.so"
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_CLASSES = 256
 MAX_PML = 4
 MAX_POLES = 8
@@ -50,16 +50,30 @@ class PointSourceC(C.Structure):
     _fields_ = [("comp", C.c_int32), ("mode", C.c_int32), ("offset", C.c_int64)]
 
 
+TFSF_MAX_FACES = 4
+
+
+class TransparentC(C.Structure):
+    _fields_ = [("comp", C.c_int32), ("nface", C.c_int32), ("offset", C.c_int64),
+                ("coef", C.c_double * TFSF_MAX_FACES), ("r0", C.c_double * TFSF_MAX_FACES),
+                ("r1", C.c_double * TFSF_MAX_FACES), ("sample", C.c_int64 * TFSF_MAX_FACES)]
+
+
 class GridDescC(C.Structure):
-    _fields_ = [
-        ("abi_version", C.c_int32), ("precision", C.c_int32), ("n", C.c_int32 * 3),
-        ("active", C.c_int32), ("naux", C.c_int32 * 6), ("nclass", C.c_int32 * 6),
-        ("npml", C.c_int32), ("nsrc", C.c_int32), ("nparam", C.c_int32),
-        ("src_steps", C.c_int32), ("flags", C.c_int32), ("reserved", C.c_int32),
-        ("dr", C.c_double * 3), ("half", C.c_double * 3), ("dt", C.c_double),
-        ("field", C.c_void_p * 6), ("cls", C.c_void_p * 6), ("aux", C.c_void_p * 6),
-        ("coef", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p),
-    ]
+    pass
+
+
+GridDescC._fields_ = [
+    ("abi_version", C.c_int32), ("precision", C.c_int32), ("n", C.c_int32 * 3),
+    ("active", C.c_int32), ("naux", C.c_int32 * 6), ("nclass", C.c_int32 * 6),
+    ("npml", C.c_int32), ("nsrc", C.c_int32), ("nparam", C.c_int32),
+    ("src_steps", C.c_int32), ("flags", C.c_int32), ("reserved", C.c_int32),
+    ("dr", C.c_double * 3), ("half", C.c_double * 3), ("dt", C.c_double),
+    ("field", C.c_void_p * 6), ("cls", C.c_void_p * 6), ("aux", C.c_void_p * 6),
+    ("coef", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p),
+    ("ntfsf", C.c_int32), ("reserved2", C.c_int32), ("tfsf", C.c_void_p),
+    ("incident", C.POINTER(GridDescC)),
+]
 
 
 class ShapeC(C.Structure):

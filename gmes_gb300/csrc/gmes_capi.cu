@@ -85,6 +85,25 @@ gmes_status check_desc(const gmes_grid_desc* g, bool need_buffers) {
   if (need_buffers && g->coef == nullptr) return fail(GMES_ERR_VALUE, "coef is NULL");
   if (need_buffers && g->nsrc > 0 && (g->src == nullptr || g->src_val == nullptr))
     return fail(GMES_ERR_VALUE, "nsrc > 0 but src or src_val is NULL");
+  if (g->ntfsf < 0) return fail(GMES_ERR_VALUE, "ntfsf = %d must be >= 0", g->ntfsf);
+  if (need_buffers && g->ntfsf > 0) {
+    const gmes_grid_desc* a = g->incident;
+    if (g->tfsf == nullptr || a == nullptr)
+      return fail(GMES_ERR_VALUE, "ntfsf > 0 but tfsf or the incident-field grid is NULL");
+    if (a->abi_version != GMES_ABI_VERSION || a->precision != g->precision || a->dt != g->dt)
+      return fail(GMES_ERR_VALUE, "the incident-field grid must share precision and dt");
+    if ((a->active & ((1 << GMES_EX) | (1 << GMES_HY))) != ((1 << GMES_EX) | (1 << GMES_HY)) ||
+        a->incident != nullptr || a->ntfsf != 0)
+      return fail(GMES_ERR_VALUE, "the incident-field grid must be a plain Ex/Hy grid");
+  }
+  return GMES_OK;
+}
+
+// The incident-field grid's own checks (without recursion into TFSF).
+gmes_status check_aux(const gmes_grid_desc* g) {
+  if (g->ntfsf == 0 || g->incident == nullptr) return GMES_OK;
+  gmes_status st = check_desc(g->incident, true);
+  if (st != GMES_OK) return fail(st, "incident-field grid: %s", g_last_error.c_str());
   return GMES_OK;
 }
 
@@ -122,6 +141,17 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
   }
   d.src = g.src;
   d.src_val = g.src_val;
+  if (g.ntfsf > 0 && g.incident != nullptr) {
+    d.tfsf = g.tfsf;
+    d.ntfsf = g.ntfsf;
+    d.tf_field[0] = g.incident->field[GMES_HY];
+    d.tf_field[1] = g.incident->field[GMES_EX];
+    for (int k = 0; k < 2; ++k) {
+      int64_t sh[3];
+      comp_shape(g.incident->n, g.incident->active, k == 0 ? GMES_HY : GMES_EX, sh);
+      d.tf_npts[k] = sh[0] * sh[1] * sh[2];
+    }
+  }
   return d;
 }
 
@@ -386,9 +416,21 @@ gmes_status gmes_step(const gmes_grid_desc* g, int32_t nsteps, void* stream) {
   if (g->nsrc > 0 && nsteps > g->src_steps)
     return fail(GMES_ERR_VALUE, "nsteps = %d exceeds the source-value capacity %d", nsteps,
                 g->src_steps);
+  st = check_aux(g);
+  if (st != GMES_OK) return st;
+  if (g->ntfsf > 0 && g->incident->nsrc > 0 && nsteps > g->incident->src_steps)
+    return fail(GMES_ERR_VALUE, "nsteps = %d exceeds the incident grid's source capacity %d",
+                nsteps, g->incident->src_steps);
   if (nsteps == 0) return GMES_OK;
   const GridDev d = make_grid_dev(*g);
-  cudaError_t e = launch_step(*g, d, nsteps, static_cast<cudaStream_t>(stream));
+  cudaError_t e;
+  if (g->ntfsf > 0) {
+    const GridDev a = make_grid_dev(*g->incident);
+    e = launch_step(*g, d, nsteps, static_cast<cudaStream_t>(stream), &a,
+                    (g->incident->flags & GMES_FLAG_DISPERSIVE) != 0);
+  } else {
+    e = launch_step(*g, d, nsteps, static_cast<cudaStream_t>(stream));
+  }
   if (e != cudaSuccess) return cuda_fail(e, "launching step kernels");
   return GMES_OK;
 }
@@ -400,8 +442,19 @@ gmes_status gmes_half_step(const gmes_grid_desc* g, int32_t side, int32_t step, 
   if (step < 0 || (g->nsrc > 0 && step >= g->src_steps))
     return fail(GMES_ERR_INDEX, "step %d outside the source-value buffer (%d steps)", step,
                 g->src_steps);
+  st = check_aux(g);
+  if (st != GMES_OK) return st;
+  if (g->ntfsf > 0 && g->incident->nsrc > 0 && step >= g->incident->src_steps)
+    return fail(GMES_ERR_INDEX, "step %d outside the incident grid's source-value buffer", step);
   const GridDev d = make_grid_dev(*g);
-  cudaError_t e = launch_half(*g, d, side, step, static_cast<cudaStream_t>(stream));
+  cudaError_t e;
+  if (g->ntfsf > 0) {
+    const GridDev a = make_grid_dev(*g->incident);
+    e = launch_half(*g, d, side, step, static_cast<cudaStream_t>(stream), &a,
+                    (g->incident->flags & GMES_FLAG_DISPERSIVE) != 0);
+  } else {
+    e = launch_half(*g, d, side, step, static_cast<cudaStream_t>(stream));
+  }
   if (e != cudaSuccess) return cuda_fail(e, "launching half-step kernels");
   return GMES_OK;
 }
@@ -439,6 +492,7 @@ gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs
     const gmes_grid_desc* g = grids[q];
     gmes_status st = check_desc(g, true);
     if (st != GMES_OK) return fail(st, "grid %d: %s", q, g_last_error.c_str());
+    if (g->ntfsf > 0) return fail(GMES_ERR_VALUE, "grid %d has a TFSF source: not batchable", q);
     if (precision < 0) precision = g->precision;
     if (g->precision != precision)
       return fail(GMES_ERR_VALUE, "grid %d: all grids of a batch must share one precision", q);
@@ -902,6 +956,7 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
     const gmes_grid_desc* g = grids[q];
     gmes_status st = check_desc(g, true);
     if (st != GMES_OK) return st;
+    if (g->ntfsf > 0) return fail(GMES_ERR_VALUE, "grid %d has a TFSF source: not batchable", q);
     if (precision < 0) precision = g->precision;
     if (g->precision != precision)
       return fail(GMES_ERR_VALUE, "grid %d: all grids must share one precision", q);

@@ -147,6 +147,13 @@ struct GridDev {
   double dr[3];
   double dt;
   Coef rdr[3];            // 1 / dr, computed on the host
+  // TFSF plane-wave source: transparent points and the incident-field
+  // arrays they sample (the aux grid's Hy for the E side, Ex for the H side)
+  const gmes_transparent* tfsf;
+  int32_t ntfsf;
+  int32_t pad2;
+  const void* tf_field[2];
+  int64_t tf_npts[2];
 };
 
 // ---------------------------------------------------------------------------
@@ -304,10 +311,12 @@ cudaError_t launch_tmz_objective(const GridDev& g, const TmzDev& t, int nsteps, 
 GridDev make_grid_dev(const gmes_grid_desc& g);
 
 // Launchers implemented per precision in gmes_step.cu.
+// aux: the incident-field grid of a TFSF source (or null), stepped between
+// the E and H halves of every step.
 cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps,
-                        cudaStream_t s);
+                        cudaStream_t s, const GridDev* aux = nullptr, bool aux_disp = false);
 cudaError_t launch_half(const gmes_grid_desc& g, const GridDev& d, int side, int step,
-                        cudaStream_t s);
+                        cudaStream_t s, const GridDev* aux = nullptr, bool aux_disp = false);
 cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nsteps, int blocks,
                          cudaStream_t s);
 cudaError_t launch_raster(const gmes_grid_desc& gd, const GridDev& d, int c,

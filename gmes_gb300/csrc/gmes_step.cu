@@ -554,6 +554,50 @@ __global__ void k_sources(const GridDev g, int side, int64_t slot) {
   source_point<P, STRICT>(g, side, slot, q);
 }
 
+// TFSF consistency corrections of one half (gmes/pw_source.py:134-486):
+// after the material update and the point sources, every face of a
+// transparent point adds coef * (r0 A[s] + r1 A[s+1]) in face order, A the
+// incident-field grid's Hy (E side) or Ex (H side).  Strict: the
+// reference's operation order (coef is the signed dt/(eps d) * amp).
+template <class P, bool STRICT>
+__global__ void k_transparent(const GridDev g, int side) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= g.ntfsf) return;
+  const gmes_transparent& t = g.tfsf[q];
+  const int c = __ldg(&t.comp);
+  if (c < 0 || c > 5 || !(g.active & (1 << c)) || (c < 3) != (side == 0)) return;
+  const int64_t off = __ldg(&t.offset);
+  if (off < 0 || off >= g.npts[c]) return;
+  const int nf = __ldg(&t.nface);
+  using T = typename P::T;
+  using R = typename P::R;
+  const T* A = static_cast<const T*>(g.tf_field[side]);
+  const int64_t na = g.tf_npts[side];
+  T* f = static_cast<T*>(g.f[c]) + off;
+  if constexpr (STRICT) {
+    double v = *reinterpret_cast<double*>(f);
+    const double* a = reinterpret_cast<const double*>(A);
+    for (int k = 0; k < nf && k < GMES_TFSF_MAX_FACES; ++k) {
+      const int64_t sp = __ldg(&t.sample[k]);
+      if (sp < 0 || sp + 1 >= na) continue;
+      const double inc = __dadd_rn(__dmul_rn(__ldg(&t.r0[k]), a[sp]),
+                                   __dmul_rn(__ldg(&t.r1[k]), a[sp + 1]));
+      v = __dadd_rn(v, __dmul_rn(__ldg(&t.coef[k]), inc));
+    }
+    *reinterpret_cast<double*>(f) = v;
+  } else {
+    R v = P::ldw(f);
+    for (int k = 0; k < nf && k < GMES_TFSF_MAX_FACES; ++k) {
+      const int64_t sp = __ldg(&t.sample[k]);
+      if (sp < 0 || sp + 1 >= na) continue;
+      const R inc = P::from_double(__ldg(&t.r0[k])) * P::ldw(A + sp) +
+                    P::from_double(__ldg(&t.r1[k])) * P::ldw(A + sp + 1);
+      v = v + P::from_double(__ldg(&t.coef[k])) * inc;
+    }
+    P::st(f, v);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Multi-grid ("batch") form: one launch per half-step advances every grid of
 // a batch.  The per-grid views live in a caller-allocated workspace with
@@ -616,10 +660,17 @@ __global__ void k_multi_sources(const BatchView v, int side, int s) {
   }
 }
 
-// One half-step: ghost copy of the other half's components, the fused
-// update of this half's components, this half's point sources.
 template <class P, bool STRICT>
-void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp) {
+cudaError_t run_steps(const GridDev& d, int nsteps, int side_mask, int st0, cudaStream_t s,
+                      bool disp, const GridDev* aux = nullptr, bool aux_disp = false);
+
+// One half-step: ghost copy of the other half's components, the fused
+// update of this half's components, this half's point sources and TFSF
+// corrections; after the E half, one full step of the TFSF incident-field
+// grid (FDTD.step's _step_aux_fdtd, gmes/fdtd.py:1113).
+template <class P, bool STRICT>
+void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp,
+              const GridDev* aux, bool aux_disp) {
   using T = typename P::T;
   int64_t maxplane = 1;
   for (int c = 0; c < 6; ++c)
@@ -645,36 +696,39 @@ void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp) {
   }
   if (d.nsrc > 0)
     k_sources<P, STRICT><<<(d.nsrc + 127) / 128, 128, 0, s>>>(d, side, 2 * (int64_t)st + side);
+  if (d.ntfsf > 0) k_transparent<P, STRICT><<<(d.ntfsf + 127) / 128, 128, 0, s>>>(d, side);
+  if (side == 0 && aux != nullptr) run_steps<P, STRICT>(*aux, 1, 3, st, s, aux_disp);
 }
 
 template <class P, bool STRICT>
 cudaError_t run_steps(const GridDev& d, int nsteps, int side_mask, int st0, cudaStream_t s,
-                      bool disp) {
+                      bool disp, const GridDev* aux, bool aux_disp) {
   for (int st = 0; st < nsteps; ++st) {
-    if (side_mask & 1) run_half<P, STRICT>(d, 0, st0 + st, s, disp);
-    if (side_mask & 2) run_half<P, STRICT>(d, 1, st0 + st, s, disp);
+    if (side_mask & 1) run_half<P, STRICT>(d, 0, st0 + st, s, disp, aux, aux_disp);
+    if (side_mask & 2) run_half<P, STRICT>(d, 1, st0 + st, s, disp, aux, aux_disp);
   }
   return cudaGetLastError();
 }
 
 template <class P, bool STRICT>
 cudaError_t dispatch(const gmes_grid_desc& g, const GridDev& d, int nsteps, int side_mask,
-                     int st0, cudaStream_t s) {
+                     int st0, cudaStream_t s, const GridDev* aux, bool aux_disp) {
   const bool disp = (g.flags & GMES_FLAG_DISPERSIVE) != 0;
-  return run_steps<P, STRICT>(d, nsteps, side_mask, st0, s, disp);
+  return run_steps<P, STRICT>(d, nsteps, side_mask, st0, s, disp, aux, aux_disp);
 }
 
 cudaError_t dispatch_precision(const gmes_grid_desc& g, const GridDev& d, int nsteps,
-                               int side_mask, int st0, cudaStream_t s) {
+                               int side_mask, int st0, cudaStream_t s, const GridDev* aux,
+                               bool aux_disp) {
   switch (g.precision) {
     case GMES_FP64:
-      return dispatch<PolF64, false>(g, d, nsteps, side_mask, st0, s);
+      return dispatch<PolF64, false>(g, d, nsteps, side_mask, st0, s, aux, aux_disp);
     case GMES_FP64_STRICT:
-      return dispatch<PolF64, true>(g, d, nsteps, side_mask, st0, s);
+      return dispatch<PolF64, true>(g, d, nsteps, side_mask, st0, s, aux, aux_disp);
     case GMES_FP32:
-      return dispatch<PolF32, false>(g, d, nsteps, side_mask, st0, s);
+      return dispatch<PolF32, false>(g, d, nsteps, side_mask, st0, s, aux, aux_disp);
     case GMES_DF64:
-      return dispatch<PolDF, false>(g, d, nsteps, side_mask, st0, s);
+      return dispatch<PolDF, false>(g, d, nsteps, side_mask, st0, s, aux, aux_disp);
     default:
       return cudaErrorInvalidValue;
   }
@@ -723,13 +777,14 @@ cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nstep
   }
 }
 
-cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps, cudaStream_t s) {
-  return dispatch_precision(g, d, nsteps, 3, 0, s);
+cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps, cudaStream_t s,
+                        const GridDev* aux, bool aux_disp) {
+  return dispatch_precision(g, d, nsteps, 3, 0, s, aux, aux_disp);
 }
 
 cudaError_t launch_half(const gmes_grid_desc& g, const GridDev& d, int side, int step,
-                        cudaStream_t s) {
-  return dispatch_precision(g, d, 1, side == 0 ? 1 : 2, step, s);
+                        cudaStream_t s, const GridDev* aux, bool aux_disp) {
+  return dispatch_precision(g, d, 1, side == 0 ? 1 : 2, step, s, aux, aux_disp);
 }
 
 }  // namespace gmes

@@ -112,6 +112,24 @@ class GridEngine:
             d.src_val = self.src_val.data_ptr()
         else:
             self.src = self.src_val = self.src_host = None
+        # TFSF: the incident-field grid (advanced inside this grid's step) and
+        # the transparent points
+        self.incident = None
+        self.tfsf = None
+        if scene.tfsf is not None:
+            aux_scene, points = scene.tfsf
+            self.incident = GridEngine(aux_scene, precision=precision, device=device,
+                                       src_chunk=src_chunk, use_graphs=False)
+            arr = (N.TransparentC * max(1, len(points)))()
+            for q, (c, off, faces) in enumerate(points):
+                t = arr[q]
+                t.comp, t.nface, t.offset = c, len(faces), off
+                for k, (cf, a, b, sp) in enumerate(faces):
+                    t.coef[k], t.r0[k], t.r1[k], t.sample[k] = cf, a, b, sp
+            self.tfsf = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev)
+            d.ntfsf = len(points)
+            d.tfsf = self.tfsf.data_ptr()
+            d.incident = C.pointer(self.incident.desc)
         self.desc = d
         self._staged = None
         self._rows, self._pool, self._pmls = rows, pool, pmls
@@ -242,6 +260,8 @@ class GridEngine:
     def reset(self):
         self._enter()
         N.check(self.lib.gmes_reset(C.byref(self.desc), C.c_void_p(self.stream)))
+        if self.incident is not None:
+            N.check(self.lib.gmes_reset(C.byref(self.incident.desc), C.c_void_p(self.stream)))
         self._leave()
 
     # -- stepping ----------------------------------------------------------
@@ -261,17 +281,24 @@ class GridEngine:
         else:
             N.check(self.lib.gmes_step(C.byref(self.desc), int(nsteps), C.c_void_p(self.stream)))
 
-    def _stage(self, vals, k):
+    def _stage(self, vals, k, stream=None):
         torch = _torch()
+        stream = stream if stream is not None else self._stream
         # the pinned staging buffer may still be read by the previous
         # chunk's asynchronous copy
         if self._staged is not None:
             self._staged.synchronize()
         self.src_host[:k].copy_(torch.from_numpy(np.ascontiguousarray(vals)))
-        with torch.cuda.stream(self._stream):
+        with torch.cuda.stream(stream):
             self.src_val[:k].copy_(self.src_host[:k], non_blocking=True)
             self._staged = torch.cuda.Event()
-            self._staged.record(self._stream)
+            self._staged.record(stream)
+
+    def _stage_incident(self, n0, k):
+        """Stage the incident-field grid's source values on this grid's stream."""
+        inc = self.incident
+        if inc is not None and inc.src is not None:
+            inc._stage(source_values(inc.scene, inc.scene.dt, n0, k), k, self._stream)
 
     def step(self, nsteps, n0=0.0, src_values=None):
         """Advance ``nsteps`` steps; the first E half-step is at n0 + 1/2.
@@ -290,6 +317,7 @@ class GridEngine:
                 vals = (src_values[done:done + k] if src_values is not None else
                         source_values(self.scene, self.scene.dt, n0 + done, k))
                 self._stage(vals, k)
+            self._stage_incident(n0 + done, k)
             self._launch(k)
             done += k
         self._leave()
@@ -301,11 +329,12 @@ class GridEngine:
 
     def stage_sources(self, n0, nsteps):
         """Stage the source values of ``nsteps`` steps from time step n0 (<= src_chunk)."""
-        if self.src is None:
-            return
         if nsteps > self.src_chunk:
             raise ValueError("more steps than the staging buffer holds")
         self._enter()
+        self._stage_incident(n0, nsteps)
+        if self.src is None:
+            return
         self._stage(source_values(self.scene, self.scene.dt, n0, nsteps), nsteps)
 
     def launch_raw(self, nsteps):

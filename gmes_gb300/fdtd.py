@@ -231,6 +231,11 @@ class FDTD:
                 "PointSource" + side[c < 3]: _PwSummary(
                     "PointSource" + side[c < 3],
                     sum(1 for s in self._scene.sources if s.comp.index == c))}
+            if self._scene.tfsf is not None:
+                n = sum(1 for q in self._scene.tfsf[1] if q[0] == c)
+                if n:
+                    name = "Transparent" + side[c < 3]
+                    self.pw_source[comp][name] = _PwSummary(name, n)
 
     @property
     def engine(self):
@@ -336,10 +341,14 @@ class FDTD:
         memo[id(self)] = new
         if self._engine is not None:
             new.init()
-            for c in range(6):
-                new._engine.fields[c].copy_(self._engine.fields[c])
-                if self._engine.aux[c] is not None:
-                    new._engine.aux[c].copy_(self._engine.aux[c])
+            pairs = [(new._engine, self._engine)]
+            if self._engine.incident is not None:
+                pairs.append((new._engine.incident, self._engine.incident))
+            for dst, src in pairs:
+                for c in range(6):
+                    dst.fields[c].copy_(src.fields[c])
+                    if src.aux[c] is not None:
+                        dst.aux[c].copy_(src.aux[c])
         new.time_step = deepcopy(self.time_step, memo)
         return new
 

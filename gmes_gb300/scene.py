@@ -61,6 +61,7 @@ class Scene:
         self.classes = [[] for _ in range(6)]
         self.pmls = []
         self.sources = []
+        self.tfsf = None      # (incident Scene, [(comp, offset, faces)]) of a TFSF source
         self.shapes = None
         self._geom = None
         self._space = None
@@ -184,7 +185,13 @@ def compile_scene(space, geom_list, e_comps, h_comps, src_list, geom_tree, dt):
     # point sources: a later source at the same point replaces an earlier
     # one, as PwSource.attach/merge do (gmes/pw_source.py:25-36)
     specs = {}
+    from .source import TotalFieldScatteredField
     for src in src_list:
+        if isinstance(src, TotalFieldScatteredField):
+            if scene.tfsf is not None:
+                raise NotImplementedError("one TotalFieldScatteredField source per simulation")
+            scene.tfsf = _compile_tfsf(src, scene, space, geom_tree, active)
+            continue
         if not hasattr(src, "resolve"):
             raise NotImplementedError(f"{type(src).__name__} is not supported by the GPU engine")
         for comp in active:
@@ -193,6 +200,21 @@ def compile_scene(space, geom_list, e_comps, h_comps, src_list, geom_tree, dt):
                 specs[(comp.index, spec.idx)] = spec
     scene.sources = list(specs.values())
     return scene
+
+
+def _compile_tfsf(src, scene, space, geom_tree, active):
+    """Incident-field scene and transparent points of a TFSF source."""
+    from .tfsf import transparent_points
+    aux = src.aux_fdtd.compile()
+    aux_shapes = [aux.shape(c) for c in range(6)]
+    points = []
+    for comp in active:
+        c = comp.index
+        sh = scene.shape(c)
+        for off, faces in transparent_points(src, comp, sh, space, scene._geom,
+                                             src.aux_fdtd.space, aux_shapes).items():
+            points.append((c, int(off), faces))
+    return aux, points
 
 
 def class_arrays(scene):

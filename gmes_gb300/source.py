@@ -167,10 +167,49 @@ class PointSource(Src):
 
 
 class TotalFieldScatteredField(Src):
-    """Plane-wave TFSF source; not yet available on the GPU engine."""
+    """Plane wave launched through the faces of a box (gmes/source.py:370-1522).
 
-    def __init__(self, *args, **kwargs):
-        raise NotImplementedError("TotalFieldScatteredField is not implemented yet")
+    ``center``, ``size``: the total-field box; ``direction``: propagation
+    direction; ``polarization``: E-field direction; ``amp``: amplitude.  The
+    incident wave is carried by a 1-D TEMz grid with a cell size matched to
+    the numerical dispersion (``gmes_gb300.tfsf``), stepped on the GPU
+    between the E and H halves of every step.
+    """
+
+    def __init__(self, src_time, center, size, direction, polarization, amp=1):
+        if not isinstance(src_time, SrcTime):
+            raise TypeError("src_time must be an instance of SrcTime.")
+        self.src_time = src_time
+        self.k = np.array(direction, np.double) / np.linalg.norm(direction)
+        self.center = np.array(center, np.double)
+        if not np.isfinite(self.center).all():
+            raise ValueError("center must contain only finite values")
+        self.size = np.array(size, np.double)
+        if not np.isfinite(self.size).all():
+            raise ValueError("size must contain only finite values")
+        self.half_size = 0.5 * self.size
+        self.e_direction = np.array(polarization, np.double) / np.linalg.norm(polarization)
+        self.h_direction = np.cross(self.k, self.e_direction)
+        self.amp = float(amp)
+        self.aux_fdtd = None
+
+    def init(self, geom_tree, space, cmplx):
+        from .tfsf import incident_grid
+        self.geom_tree = geom_tree
+        self.src_time.init(cmplx)
+        self.aux_fdtd = incident_grid(self, space, geom_tree)
+
+    def display_info(self, indent=0):
+        print(" " * indent, "plane-wave source:")
+        print(" " * indent, "propagation direction:", self.k)
+        print(" " * indent, "center:", self.center)
+        print(" " * indent, "source plane size:", self.size)
+        print(" " * indent, "polarization direction:", self.e_direction)
+        print(" " * indent, "amplitude:", self.amp)
+        self.src_time.display_info(4)
+
+    def mode_function(self, x, y, z):
+        return 1.0
 
 
 class GaussianBeam(Src):

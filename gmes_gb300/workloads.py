@@ -12,7 +12,8 @@ distributions of the benchmark configurations:
 * ``dispersive`` 3-D N^3 (default 192^3) in eps = 2.25: a 4x4 lattice of
                 Drude spheres (omega_p 9, gamma 0.07, radius 10-20 cells), a
                 Lorentz slab (2.0, 3.0, 0.1), a DCP-ADE sphere (1 Drude term +
-                2 seeded critical points), 12-cell UPML, 2000 steps.
+                2 seeded critical points), 12-cell UPML, a TFSF plane wave
+                (+z, x-polarised, Bandpass(0.5, 0.2)), 2000 steps.
 * ``design2d``  2-D TMz N^2 (default 512^2) differentiation scene: vacuum,
                 20-cell CPML, an Ez-polarised line source (a column of Jz
                 point sources, Bandpass(0.5, 0.5)) left of a 64x64-point
@@ -24,7 +25,7 @@ import numpy as np
 
 from . import (Bandpass, Block, Cartesian, Continuous, Cpml, CriticalPoint, DcpAde,
                DefaultMedium, Dielectric, Drude, DrudePole, Ex, Ez, FDTD, Jz, Lorentz,
-               LorentzPole, PointSource, Shell, Sphere, TMzFDTD, Upml)
+               LorentzPole, PointSource, Shell, Sphere, TMzFDTD, TotalFieldScatteredField, Upml)
 
 
 def air2d(precision="fp64", verbose=False):
@@ -63,13 +64,14 @@ def cube(n=256, nobj=24, seed=0, pml_cells=10, precision="fp64", verbose=False, 
 
 
 def dispersive(n=192, seed=0, pml_cells=12, precision="fp64", verbose=False, res=20,
-               courant_ratio=0.6, src_time=None):
+               courant_ratio=0.6, src_time=None, tfsf=True):
     """The 3-D dispersive + UPML benchmark scene on an n^3 grid (resolution 20).
 
     dt follows the background medium (eps = 2.25) as in the reference, so
     the Courant ratio is lowered to 0.6 to keep the eps_inf = 1 metal stable.
-    The plane-wave (TFSF) excitation of the benchmark is replaced by an Ez
-    point source until the TFSF source runs on the GPU.
+    Excitation: a +z plane wave, x-polarised, Bandpass(0.5, 0.2), through a
+    TFSF box spanning 90% of the PML-free interior (``tfsf=False``: an Ez
+    point source at the centre instead).
     """
     rng = np.random.default_rng(seed)
     dx = 1.0 / res
@@ -94,8 +96,13 @@ def dispersive(n=192, seed=0, pml_cells=12, precision="fp64", verbose=False, res
                                        cps=cps),
                        center=(0.4 * inner, -0.4 * inner, 0.7 * inner), radius=0.2 * inner))
     geom.append(Shell(material=Upml(), thickness=pml_cells * dx))
-    src = [PointSource(src_time=src_time or Bandpass(freq=0.5, fwidth=0.2), center=(0, 0, 0),
-                       component=Ez)]
+    st = src_time or Bandpass(freq=0.5, fwidth=0.2)
+    if tfsf:
+        box = 2 * inner * 0.9
+        src = [TotalFieldScatteredField(src_time=st, center=(0, 0, 0), size=(box, box, box),
+                                        direction=(0, 0, 1), polarization=(1, 0, 0))]
+    else:
+        src = [PointSource(src_time=st, center=(0, 0, 0), component=Ez)]
     space = Cartesian(size=(size, size, size), resolution=res)
     return FDTD(space, geom, src, verbose=verbose, precision=precision,
                 courant_ratio=courant_ratio), 2000

@@ -46,7 +46,7 @@
 extern "C" {
 #endif
 
-#define GMES_ABI_VERSION 1
+#define GMES_ABI_VERSION 2
 #define GMES_MAX_CLASSES 256 /* class ids are u8 */
 #define GMES_MAX_PML 4       /* PML materials per grid */
 #define GMES_MAX_POLES 8     /* Drude/Lorentz poles, DCP terms per class */
@@ -121,6 +121,27 @@ typedef struct {
   double half_size[3];  /* +inf on an axis whose half size is below d */
 } gmes_pml_desc;
 
+/*
+ * One point of a total-field/scattered-field (TFSF) plane-wave source: the
+ * consistency corrections of the reference's Transparent{E,H}? sources
+ * (gmes/pw_source.py:134-486) at a point of the TFSF box faces.  After the
+ * material update and the point sources of its half, face f adds
+ *     field += coef[f] * (r0[f] * A[sample[f]] + r1[f] * A[sample[f] + 1])
+ * in face order, where A is the incident-field grid's Hy array for an E
+ * point and its Ex array for an H point; coef[f] is the signed
+ * dt / (eps_or_mu * d) * amp of that face (gmes/source.py:616-665).
+ */
+#define GMES_TFSF_MAX_FACES 4
+typedef struct {
+  int32_t comp;     /* field component of the point */
+  int32_t nface;    /* 1 .. GMES_TFSF_MAX_FACES */
+  int64_t offset;   /* linear index into the component's array */
+  double coef[GMES_TFSF_MAX_FACES];
+  double r0[GMES_TFSF_MAX_FACES];
+  double r1[GMES_TFSF_MAX_FACES];
+  int64_t sample[GMES_TFSF_MAX_FACES];
+} gmes_transparent;
+
 /* One point source, resolved to one Yee point (gmes/pw_source.py:74-131). */
 typedef struct {
   int32_t comp;   /* field component 0..5 */
@@ -132,7 +153,7 @@ typedef struct {
  * The grid: shape, step sizes and the caller-allocated device buffers.
  * Sizes in bytes of each buffer are given by gmes_grid_sizes().
  */
-typedef struct {
+typedef struct gmes_grid_desc {
   int32_t abi_version;   /* GMES_ABI_VERSION */
   int32_t precision;     /* gmes_precision */
   int32_t n[3];          /* Cartesian.whole_field_size */
@@ -155,6 +176,16 @@ typedef struct {
   void* coef;            /* coefficient block, written by gmes_build_coefficients */
   gmes_point_source* src;/* nsrc point sources */
   double* src_val;       /* source values, [step][source] (see gmes_step) */
+  /* TFSF plane-wave source (optional): the 1-D incident-field grid (a TEMz
+     grid, Ex and Hy, same precision and dt) is advanced one full step
+     between this grid's E and H halves, as FDTD.step does with the
+     aux_fdtd of TotalFieldScatteredField (gmes/fdtd.py:1099-1122,
+     gmes/source.py:422-425); ntfsf transparent points correct the fields
+     on the TFSF box faces.  Grids with a TFSF source cannot be batched. */
+  int32_t ntfsf;
+  int32_t reserved2;
+  gmes_transparent* tfsf;
+  const struct gmes_grid_desc* incident;
 } gmes_grid_desc;
 /*
  * State slots (naux) per kind, the same state the reference keeps inside

@@ -69,7 +69,7 @@ typedef struct {
   void* pts;
 } updater;
 
-typedef struct {
+typedef struct oracle_s {
   int n[3];
   int active;
   double dr[3], half[3], dt;
@@ -86,6 +86,17 @@ typedef struct {
   int* src_mode;
   int64_t* src_off;
   int64_t omp_threshold;
+  /* TFSF: the incident-field oracle (a TEMz grid) and the transparent
+     points, up to 4 faces each (gmes/pw_source.py:134-486) */
+  struct oracle_s* incident;
+  int ntfsf;
+  int* tf_comp;
+  int* tf_nface;
+  int64_t* tf_off;
+  double* tf_coef;  /* [ntfsf][4] */
+  double* tf_r0;
+  double* tf_r1;
+  int64_t* tf_sample;
 } oracle;
 
 static void comp_shape(const int n[3], int active, int c, int64_t sh[3]) {
@@ -593,25 +604,92 @@ static void apply_sources(oracle* o, int side, const double* vals) {
   }
 }
 
-/* src_vals: [nsteps][2][nsrc] (E value, H value per source). */
-int oracle_step(oracle* o, int nsteps, const double* src_vals) {
+/* TFSF consistency corrections of one half, each point's faces in order:
+   F -= / += dt/(eps d) * amp * (r0 A[s] + r1 A[s+1]) with A the incident
+   grid's Hy (E side) or Ex (H side); coef holds the signed
+   dt/(eps d) * amp (gmes/pw_source.py:196-486). */
+static void apply_transparent(oracle* o, int side) {
+  if (!o->incident) return;
+  const double* A = o->incident->f[side == 0 ? 4 : 0];
+  for (int q = 0; q < o->ntfsf; ++q) {
+    const int c = o->tf_comp[q];
+    if ((c < 3) != (side == 0)) continue;
+    double* f = o->f[c] + o->tf_off[q];
+    for (int k = 0; k < o->tf_nface[q]; ++k) {
+      const int64_t sp = o->tf_sample[4 * q + k];
+      const double inc = o->tf_r0[4 * q + k] * A[sp] + o->tf_r1[4 * q + k] * A[sp + 1];
+      *f = *f + o->tf_coef[4 * q + k] * inc;
+    }
+  }
+}
+
+int oracle_set_tfsf(oracle* o, oracle* incident, int n, const int* comp, const int* nface,
+                    const int64_t* off, const double* coef, const double* r0, const double* r1,
+                    const int64_t* sample) {
+  o->incident = incident;
+  o->ntfsf = n;
+  size_t m = (size_t)(n ? n : 1);
+  o->tf_comp = (int*)malloc(m * sizeof(int));
+  o->tf_nface = (int*)malloc(m * sizeof(int));
+  o->tf_off = (int64_t*)malloc(m * sizeof(int64_t));
+  o->tf_coef = (double*)malloc(4 * m * sizeof(double));
+  o->tf_r0 = (double*)malloc(4 * m * sizeof(double));
+  o->tf_r1 = (double*)malloc(4 * m * sizeof(double));
+  o->tf_sample = (int64_t*)malloc(4 * m * sizeof(int64_t));
+  if (!o->tf_comp || !o->tf_nface || !o->tf_off || !o->tf_coef || !o->tf_r0 || !o->tf_r1 ||
+      !o->tf_sample)
+    return -1;
+  const int64_t na[2] = {incident->sh[4][0] * incident->sh[4][1] * incident->sh[4][2],
+                         incident->sh[0][0] * incident->sh[0][1] * incident->sh[0][2]};
+  for (int q = 0; q < n; ++q) {
+    if (comp[q] < 0 || comp[q] > 5 || nface[q] < 1 || nface[q] > 4) return -2;
+    o->tf_comp[q] = comp[q];
+    o->tf_nface[q] = nface[q];
+    o->tf_off[q] = off[q];
+    for (int k = 0; k < 4; ++k) {
+      o->tf_coef[4 * q + k] = coef[4 * q + k];
+      o->tf_r0[4 * q + k] = r0[4 * q + k];
+      o->tf_r1[4 * q + k] = r1[4 * q + k];
+      o->tf_sample[4 * q + k] = sample[4 * q + k];
+      if (k < nface[q] && (sample[4 * q + k] < 0 || sample[4 * q + k] + 1 >= na[comp[q] < 3 ? 0 : 1]))
+        return -3;
+    }
+  }
+  return 0;
+}
+
+/* src_vals: [nsteps][2][nsrc] (E value, H value per source); aux_vals the
+   same for the incident-field grid (NULL without TFSF).  The incident grid
+   takes its full step between the E and H halves, as FDTD.step calls
+   _step_aux_fdtd (gmes/fdtd.py:1099-1122). */
+int oracle_step_tfsf(oracle* o, int nsteps, const double* src_vals, const double* aux_vals) {
+  if (o->incident && !aux_vals) return -1;
   for (int s = 0; s < nsteps; ++s) {
     for (int c = 3; c < 6; ++c) chatter(o, c);
     for (int c = 0; c < 3; ++c)
       for (int k = 0; k < o->nupd[c]; ++k) run_updater(o, &o->upd[c][k]);
     apply_sources(o, 0, src_vals + (int64_t)(2 * s) * o->nsrc);
+    apply_transparent(o, 0);
+    if (o->incident)
+      oracle_step_tfsf(o->incident, 1, aux_vals + (int64_t)(2 * s) * o->incident->nsrc, NULL);
     for (int c = 0; c < 3; ++c) chatter(o, c);
     for (int c = 3; c < 6; ++c)
       for (int k = 0; k < o->nupd[c]; ++k) run_updater(o, &o->upd[c][k]);
     apply_sources(o, 1, src_vals + (int64_t)(2 * s + 1) * o->nsrc);
+    apply_transparent(o, 1);
   }
   return 0;
+}
+
+int oracle_step(oracle* o, int nsteps, const double* src_vals) {
+  return oracle_step_tfsf(o, nsteps, src_vals, NULL);
 }
 
 /* ---- reset and per-point permittivity ------------------------------------ */
 
 /* Zero every field and every per-point state (psi, d, ADE). */
 int oracle_reset(oracle* o) {
+  if (o->incident) oracle_reset(o->incident);
   for (int c = 0; c < 6; ++c) {
     memset(o->f[c], 0, sizeof(double) * (size_t)(o->sh[c][0] * o->sh[c][1] * o->sh[c][2]));
     for (int k = 0; k < o->nupd[c]; ++k) {
@@ -776,6 +854,7 @@ static const p_diel* find_diel(const oracle* o, int c, int64_t off) {
 int oracle_adjoint(oracle* o, int nsteps, const double* src_vals, int nmon, const int* mcomp,
                    const int64_t* moff, int ndes, const int* dcomp, const int64_t* doff,
                    double* J, double* grad) {
+  if (o->incident) return -1;
   for (int c = 0; c < 6; ++c)
     for (int k = 0; k < o->nupd[c]; ++k)
       if (o->upd[c][k].kind != K_DIEL && o->upd[c][k].kind != K_CPML) return -1;
@@ -868,5 +947,7 @@ void oracle_destroy(oracle* o) {
     }
   }
   free(o->src_comp); free(o->src_mode); free(o->src_off);
+  free(o->tf_comp); free(o->tf_nface); free(o->tf_off); free(o->tf_coef);
+  free(o->tf_r0); free(o->tf_r1); free(o->tf_sample);
   free(o);
 }

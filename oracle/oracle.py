@@ -63,6 +63,12 @@ def load():
     lib.oracle_pml_profile.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P(C.c_double)]
     lib.oracle_step.restype = C.c_int
     lib.oracle_step.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
+    lib.oracle_step_tfsf.restype = C.c_int
+    lib.oracle_step_tfsf.argtypes = [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double)]
+    lib.oracle_set_tfsf.restype = C.c_int
+    lib.oracle_set_tfsf.argtypes = [C.c_void_p, C.c_void_p, C.c_int, P(C.c_int), P(C.c_int),
+                                    P(C.c_int64), P(C.c_double), P(C.c_double), P(C.c_double),
+                                    P(C.c_int64)]
     lib.oracle_threads.restype = C.c_int
     lib.oracle_reset.restype = C.c_int
     lib.oracle_reset.argtypes = [C.c_void_p]
@@ -123,6 +129,29 @@ class Oracle:
         mode = (C.c_int * max(1, len(srcs)))(*[s[1] for s in srcs])
         off = (C.c_int64 * max(1, len(srcs)))(*[s[2] for s in srcs])
         self.lib.oracle_set_sources(self.h, len(srcs), comp, mode, off)
+        self.incident = None
+        if scene.tfsf is not None:
+            aux_scene, points = scene.tfsf
+            self.incident = Oracle(aux_scene)
+            n = len(points)
+            tc = np.zeros(n, np.int32)
+            nf = np.zeros(n, np.int32)
+            to = np.zeros(n, np.int64)
+            coef = np.zeros((n, 4))
+            r0 = np.zeros((n, 4))
+            r1 = np.zeros((n, 4))
+            smp = np.zeros((n, 4), np.int64)
+            for q, (c, o_, faces) in enumerate(points):
+                tc[q], nf[q], to[q] = c, len(faces), o_
+                for k, (cf, a, b, sp) in enumerate(faces):
+                    coef[q, k], r0[q, k], r1[q, k], smp[q, k] = cf, a, b, sp
+            ip = C.POINTER(C.c_int)
+            lp = C.POINTER(C.c_int64)
+            r = self.lib.oracle_set_tfsf(self.h, self.incident.h, n, tc.ctypes.data_as(ip),
+                                         nf.ctypes.data_as(ip), to.ctypes.data_as(lp),
+                                         _dp(coef), _dp(r0), _dp(r1), smp.ctypes.data_as(lp))
+            if r != 0:
+                raise ValueError("bad TFSF table")
         self.n = 0.0
 
     def __del__(self):
@@ -137,7 +166,15 @@ class Oracle:
         v = np.ascontiguousarray(src_values, np.float64)
         if v.size == 0:
             v = np.zeros(1)
-        self.lib.oracle_step(self.h, int(nsteps), _dp(v))
+        if self.incident is not None:
+            a = np.ascontiguousarray(
+                source_values(self.incident.scene, self.scene.dt, self.n, nsteps), np.float64)
+            if a.size == 0:
+                a = np.zeros(1)
+            self.lib.oracle_step_tfsf(self.h, int(nsteps), _dp(v), _dp(a))
+            self.incident.n += nsteps
+        else:
+            self.lib.oracle_step(self.h, int(nsteps), _dp(v))
         self.n += nsteps
 
     def field(self, c):
@@ -159,6 +196,8 @@ class Oracle:
         """Zero the fields and every per-point state; time returns to 0."""
         self.lib.oracle_reset(self.h)
         self.n = 0.0
+        if self.incident is not None:
+            self.incident.n = 0.0
 
     def set_eps(self, c, points, eps):
         """Per-point permittivity of dielectric points (c, index tuples) of component c."""

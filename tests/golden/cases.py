@@ -138,6 +138,36 @@ def tmx_cpml_hard(g, steps=80):
     return g.TMxFDTD(space, geometry, sources, verbose=False), steps
 
 
+def tfsf2d(g, steps=120):
+    """TMz plane wave (+x, Ez-polarised) through a TFSF box around a dielectric
+    sphere, CPML; the incident-field grid is the reference's matched-dispersion
+    TEMz aux FDTD (gmes/source.py:579-651)."""
+    space = g.Cartesian(size=(4, 4, 0), resolution=10)
+    geometry = [g.DefaultMedium(material=g.Dielectric()),
+                g.Sphere(material=g.Dielectric(eps_inf=4.0), center=(0.3, 0, 0), radius=0.5),
+                g.Shell(material=g.Cpml(), thickness=0.6)]
+    sources = [g.TotalFieldScatteredField(src_time=g.Bandpass(freq=1.0, fwidth=1.0, s=3),
+                                          center=(0, 0, 0), size=(2.0, 2.0, 0),
+                                          direction=(1, 0, 0), polarization=(0, 0, 1))]
+    return g.TMzFDTD(space, geometry, sources, verbose=False), steps
+
+
+def tfsf3d(g, steps=60):
+    """3-D oblique plane wave through a TFSF box in an eps = 1.5 background
+    around a dielectric sphere, CPML on all faces."""
+    import numpy as np
+    space = g.Cartesian(size=(2.4, 2.4, 2.4), resolution=10)
+    geometry = [g.DefaultMedium(material=g.Dielectric(eps_inf=1.5)),
+                g.Sphere(material=g.Dielectric(eps_inf=4.0), center=(0.1, 0, 0), radius=0.3),
+                g.Shell(material=g.Cpml(), thickness=0.4)]
+    k = np.array((1.0, 0.5, 0.2))
+    pol = tuple(float(v) for v in np.cross(k / np.linalg.norm(k), (0, 0, 1)))
+    sources = [g.TotalFieldScatteredField(src_time=g.Bandpass(freq=1.0, fwidth=1.0, s=3),
+                                          center=(0, 0, 0), size=(1.2, 1.2, 1.2),
+                                          direction=tuple(k), polarization=pol)]
+    return g.FDTD(space, geometry, sources, verbose=False), steps
+
+
 CASES = {
     "tmz_regression": tmz_regression,
     "air2d": air2d,
@@ -146,6 +176,8 @@ CASES = {
     "drude2d": drude2d,
     "tez_upml_currents": tez_upml_currents,
     "tmx_cpml_hard": tmx_cpml_hard,
+    "tfsf2d": tfsf2d,
+    "tfsf3d": tfsf3d,
 }
 
 # Cases whose golden file stores only Ez in full (and checksums of the rest)

@@ -24,12 +24,16 @@ def run_case(name, precision, host_profiles=False):
     sim.precision = precision
     sim.init()
     if host_profiles:
-        orc = Oracle(sim.scene)
-        for p in range(len(sim.scene.pmls)):
-            for comp in sim.scene.active:
-                for axis in range(3):
-                    sim.engine.set_pml_profile(p, comp.index, axis,
-                                               orc.pml_profile(p, comp.index, axis))
+        engines = [(sim.engine, sim.scene)]
+        if sim.engine.incident is not None:
+            engines.append((sim.engine.incident, sim.scene.tfsf[0]))
+        for eng, scene in engines:
+            orc = Oracle(scene)
+            for p in range(len(scene.pmls)):
+                for comp in scene.active:
+                    for axis in range(3):
+                        eng.set_pml_profile(p, comp.index, axis,
+                                            orc.pml_profile(p, comp.index, axis))
     sim.step_until_n(nsteps)
     return sim, nsteps
 
