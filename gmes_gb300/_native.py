@@ -10,7 +10,7 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libgmes_gb300.so"
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_CLASSES = 256
 MAX_PML = 4
 MAX_POLES = 8
@@ -59,6 +59,10 @@ class TransparentC(C.Structure):
                 ("r1", C.c_double * TFSF_MAX_FACES), ("sample", C.c_int64 * TFSF_MAX_FACES)]
 
 
+class ProbeC(C.Structure):
+    _fields_ = [("comp", C.c_int32), ("pad", C.c_int32), ("offset", C.c_int64)]
+
+
 class GridDescC(C.Structure):
     pass
 
@@ -73,6 +77,8 @@ GridDescC._fields_ = [
     ("coef", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p),
     ("ntfsf", C.c_int32), ("reserved2", C.c_int32), ("tfsf", C.c_void_p),
     ("incident", C.POINTER(GridDescC)),
+    ("nprobe", C.c_int32), ("probe_steps", C.c_int32), ("probe", C.c_void_p),
+    ("probe_val", C.c_void_p),
 ]
 
 

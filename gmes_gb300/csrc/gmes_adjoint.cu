@@ -41,15 +41,6 @@ namespace {
 
 constexpr int kBX = 32, kBY = 8;
 
-template <class R>
-__device__ __forceinline__ double to_double(R v);
-template <>
-__device__ __forceinline__ double to_double<double>(double v) { return v; }
-template <>
-__device__ __forceinline__ double to_double<float>(float v) { return (double)v; }
-template <>
-__device__ __forceinline__ double to_double<df>(df v) { return (double)v.hi + (double)v.lo; }
-
 struct Lat {
   int i, j, b;
   int64_t base, lin;

@@ -86,6 +86,10 @@ gmes_status check_desc(const gmes_grid_desc* g, bool need_buffers) {
   if (need_buffers && g->nsrc > 0 && (g->src == nullptr || g->src_val == nullptr))
     return fail(GMES_ERR_VALUE, "nsrc > 0 but src or src_val is NULL");
   if (g->ntfsf < 0) return fail(GMES_ERR_VALUE, "ntfsf = %d must be >= 0", g->ntfsf);
+  if (g->nprobe < 0 || g->probe_steps < 0)
+    return fail(GMES_ERR_VALUE, "negative nprobe / probe_steps");
+  if (need_buffers && g->nprobe > 0 && (g->probe == nullptr || g->probe_val == nullptr))
+    return fail(GMES_ERR_VALUE, "nprobe > 0 but probe or probe_val is NULL");
   if (need_buffers && g->ntfsf > 0) {
     const gmes_grid_desc* a = g->incident;
     if (g->tfsf == nullptr || a == nullptr)
@@ -141,6 +145,11 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
   }
   d.src = g.src;
   d.src_val = g.src_val;
+  if (g.nprobe > 0) {
+    d.probe = g.probe;
+    d.probe_val = g.probe_val;
+    d.nprobe = g.nprobe;
+  }
   if (g.ntfsf > 0 && g.incident != nullptr) {
     d.tfsf = g.tfsf;
     d.ntfsf = g.ntfsf;
@@ -416,6 +425,9 @@ gmes_status gmes_step(const gmes_grid_desc* g, int32_t nsteps, void* stream) {
   if (g->nsrc > 0 && nsteps > g->src_steps)
     return fail(GMES_ERR_VALUE, "nsteps = %d exceeds the source-value capacity %d", nsteps,
                 g->src_steps);
+  if (g->nprobe > 0 && nsteps > g->probe_steps)
+    return fail(GMES_ERR_VALUE, "nsteps = %d exceeds the probe buffer capacity %d", nsteps,
+                g->probe_steps);
   st = check_aux(g);
   if (st != GMES_OK) return st;
   if (g->ntfsf > 0 && g->incident->nsrc > 0 && nsteps > g->incident->src_steps)
@@ -442,6 +454,9 @@ gmes_status gmes_half_step(const gmes_grid_desc* g, int32_t side, int32_t step, 
   if (step < 0 || (g->nsrc > 0 && step >= g->src_steps))
     return fail(GMES_ERR_INDEX, "step %d outside the source-value buffer (%d steps)", step,
                 g->src_steps);
+  if (g->nprobe > 0 && step >= g->probe_steps)
+    return fail(GMES_ERR_INDEX, "step %d outside the probe buffer (%d steps)", step,
+                g->probe_steps);
   st = check_aux(g);
   if (st != GMES_OK) return st;
   if (g->ntfsf > 0 && g->incident->nsrc > 0 && step >= g->incident->src_steps)
@@ -493,6 +508,7 @@ gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs
     gmes_status st = check_desc(g, true);
     if (st != GMES_OK) return fail(st, "grid %d: %s", q, g_last_error.c_str());
     if (g->ntfsf > 0) return fail(GMES_ERR_VALUE, "grid %d has a TFSF source: not batchable", q);
+    if (g->nprobe > 0) return fail(GMES_ERR_VALUE, "grid %d has probes: not batchable", q);
     if (precision < 0) precision = g->precision;
     if (g->precision != precision)
       return fail(GMES_ERR_VALUE, "grid %d: all grids of a batch must share one precision", q);
@@ -957,6 +973,7 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
     gmes_status st = check_desc(g, true);
     if (st != GMES_OK) return st;
     if (g->ntfsf > 0) return fail(GMES_ERR_VALUE, "grid %d has a TFSF source: not batchable", q);
+    if (g->nprobe > 0) return fail(GMES_ERR_VALUE, "grid %d has probes: not batchable", q);
     if (precision < 0) precision = g->precision;
     if (g->precision != precision)
       return fail(GMES_ERR_VALUE, "grid %d: all grids must share one precision", q);

@@ -154,6 +154,11 @@ struct GridDev {
   int32_t pad2;
   const void* tf_field[2];
   int64_t tf_npts[2];
+  // probes: values recorded per step of a call
+  const gmes_probe* probe;
+  double* probe_val;
+  int32_t nprobe;
+  int32_t pad3;
 };
 
 // ---------------------------------------------------------------------------
@@ -247,6 +252,11 @@ struct PolDF {
     return {h, static_cast<float>(v - static_cast<double>(h))};
   }
 };
+
+// FP64 value of an arithmetic-policy number (records, gradients).
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(float v) { return (double)v; }
+__device__ __forceinline__ double to_double(df v) { return (double)v.hi + (double)v.lo; }
 
 // Threads per block of the half-step kernels (single grid and batch).
 constexpr int kBatchThreads = 256;

@@ -598,6 +598,20 @@ __global__ void k_transparent(const GridDev g, int side) {
   }
 }
 
+// Probe recording of one half: the value of every probe of this half's
+// components after its updates, sources and TFSF corrections.
+template <class P>
+__global__ void k_probes(const GridDev g, int side, int64_t slot) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= g.nprobe) return;
+  const gmes_probe pr = g.probe[q];
+  if (pr.comp < 0 || pr.comp > 5 || (pr.comp < 3) != (side == 0)) return;
+  double v = 0.0;
+  if ((g.active & (1 << pr.comp)) && pr.offset >= 0 && pr.offset < g.npts[pr.comp])
+    v = to_double(P::ldw(static_cast<const typename P::T*>(g.f[pr.comp]) + pr.offset));
+  g.probe_val[slot * g.nprobe + q] = v;
+}
+
 // ---------------------------------------------------------------------------
 // Multi-grid ("batch") form: one launch per half-step advances every grid of
 // a batch.  The per-grid views live in a caller-allocated workspace with
@@ -697,6 +711,7 @@ void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp,
   if (d.nsrc > 0)
     k_sources<P, STRICT><<<(d.nsrc + 127) / 128, 128, 0, s>>>(d, side, 2 * (int64_t)st + side);
   if (d.ntfsf > 0) k_transparent<P, STRICT><<<(d.ntfsf + 127) / 128, 128, 0, s>>>(d, side);
+  if (d.nprobe > 0) k_probes<P><<<(d.nprobe + 127) / 128, 128, 0, s>>>(d, side, st);
   if (side == 0 && aux != nullptr) run_steps<P, STRICT>(*aux, 1, 3, st, s, aux_disp);
 }
 

@@ -130,6 +130,8 @@ class GridEngine:
             d.ntfsf = len(points)
             d.tfsf = self.tfsf.data_ptr()
             d.incident = C.pointer(self.incident.desc)
+        self.probes = None
+        self.probe_val = None
         self.desc = d
         self._staged = None
         self._rows, self._pool, self._pmls = rows, pool, pmls
@@ -264,6 +266,36 @@ class GridEngine:
             N.check(self.lib.gmes_reset(C.byref(self.incident.desc), C.c_void_p(self.stream)))
         self._leave()
 
+    # -- probes ------------------------------------------------------------
+    def set_probes(self, points):
+        """Record the value of every (component, flat offset) point after each
+        half-step (per step, into a device buffer read by ``probe_values``)."""
+        torch = _torch()
+        points = list(points)
+        d = self.desc
+        if not points:
+            d.nprobe, d.probe, d.probe_val = 0, None, None
+            self.probes = self.probe_val = None
+        else:
+            arr = (N.ProbeC * len(points))(*[N.ProbeC(c, 0, o) for c, o in points])
+            self.probes = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(
+                self.device)
+            self.probe_val = torch.zeros((self.src_chunk, len(points)), dtype=torch.float64,
+                                         device=self.device)
+            d.nprobe = len(points)
+            d.probe_steps = self.src_chunk
+            d.probe = self.probes.data_ptr()
+            d.probe_val = self.probe_val.data_ptr()
+        # captured graphs hold the old descriptor
+        for h in self._graphs.values():
+            self.lib.gmes_graph_destroy(h)
+        self._graphs.clear()
+
+    def probe_values(self, k):
+        """(k, nprobe) float64 numpy: the probes of the last k recorded steps of a chunk."""
+        self._stream.synchronize()
+        return self.probe_val[:k].cpu().numpy()
+
     # -- stepping ----------------------------------------------------------
     def _graph(self, nsteps):
         h = self._graphs.get(nsteps)
@@ -300,7 +332,7 @@ class GridEngine:
         if inc is not None and inc.src is not None:
             inc._stage(source_values(inc.scene, inc.scene.dt, n0, k), k, self._stream)
 
-    def step(self, nsteps, n0=0.0, src_values=None):
+    def step(self, nsteps, n0=0.0, src_values=None, on_chunk=None):
         """Advance ``nsteps`` steps; the first E half-step is at n0 + 1/2.
 
         Steps run in chunks of up to ``src_chunk``: the source values of a
@@ -319,6 +351,8 @@ class GridEngine:
                 self._stage(vals, k)
             self._stage_incident(n0 + done, k)
             self._launch(k)
+            if on_chunk is not None:
+                on_chunk(done, k)
             done += k
         self._leave()
 

@@ -167,6 +167,7 @@ class FDTD:
         self.h_recorder = []
         self._engine = None
         self._scene = None
+        self._probes_set = 0
 
     def _init_field_compnt(self):
         self.e_field_compnt = (Ex, Ey, Ez)
@@ -252,17 +253,23 @@ class FDTD:
         if nsteps <= 0:
             return
         n0 = self.time_step.n
-        if self.e_recorder or self.h_recorder:
-            for _ in range(nsteps):
-                self._engine.step(1, n0=self.time_step.n)
-                self.time_step.half_step_up()
-                for probe in self.e_recorder:
-                    probe.write(self.time_step.n - 0.5)
-                self.time_step.half_step_up()
-                for probe in self.h_recorder:
-                    probe.write(self.time_step.n)
-            return
-        self._engine.step(nsteps, n0=n0)
+        probes = self.e_recorder + self.h_recorder
+        if probes:
+            if self._engine.probes is None or self._probes_set != len(probes):
+                self._engine.set_probes([(p.c, p.offset) for p in probes])
+                self._probes_set = len(probes)
+
+            def flush(done, k):
+                vals = self._engine.probe_values(k)
+                for s in range(k):
+                    n = n0 + (done + s)
+                    for q, p in enumerate(probes):
+                        p.write(n + (0.5 if p.c < 3 else 1.0), vals[s, q])
+                for p in probes:
+                    p.f.flush()
+            self._engine.step(nsteps, n0=n0, on_chunk=flush)
+        else:
+            self._engine.step(nsteps, n0=n0)
         for _ in range(nsteps):
             self.time_step.half_step_up()
             self.time_step.half_step_up()
@@ -316,6 +323,7 @@ class FDTD:
             if in_range(idx, self.field[comp].shape, comp):
                 rec = _Probe(self, comp, idx, (prefix or "") + postfix[comp])
                 rec.write_header(self.space.index_to_space(comp, *idx), self.time_step.dt)
+                rec.f.flush()
                 (self.e_recorder if comp.index < 3 else self.h_recorder).append(rec)
 
     def write_field(self, comp, low=None, high=None, prefix=None, postfix=None):
@@ -354,20 +362,32 @@ class FDTD:
 
 
 class _Probe:
-    """Per-step field recorder (gmes/file_io.py:9-48)."""
+    """Per-step field recorder writing the reference's text format
+    (gmes/file_io.py:9-48): a header, then "n value" per step.  Values come
+    from the engine's device probe buffer, one read per chunk of steps."""
 
     def __init__(self, sim, comp, idx, filename):
         self.sim, self.c, self.idx = sim, comp.index, tuple(int(i) for i in idx)
+        sh = sim._scene.shape(self.c) if sim._scene is not None else sim.field[comp].shape
+        self.offset = int(np.ravel_multi_index(self.idx, sh))
         self.f = open(filename, "w")
 
     def write_header(self, loc, dt):
-        self.f.write("# location=" + str(tuple(float(v) for v in loc)) + "\n")
+        self.f.write("# location=" + str(loc) + "\n")
         self.f.write("# dt=" + str(dt) + "\n")
 
-    def write(self, n):
-        value = float(self.sim._engine.read_tensor(self.c)[self.idx].item())
-        self.f.write(f"{n}\t{value}\n")
-        self.f.flush()
+    def write(self, n, value):
+        self.f.write(str(n) + " " + str(np.float64(value)) + "\n")
+
+    def close(self):
+        if not self.f.closed:
+            self.f.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _mode(name, e, h, doc):

@@ -46,7 +46,7 @@
 extern "C" {
 #endif
 
-#define GMES_ABI_VERSION 2
+#define GMES_ABI_VERSION 3
 #define GMES_MAX_CLASSES 256 /* class ids are u8 */
 #define GMES_MAX_PML 4       /* PML materials per grid */
 #define GMES_MAX_POLES 8     /* Drude/Lorentz poles, DCP terms per class */
@@ -142,6 +142,13 @@ typedef struct {
   int64_t sample[GMES_TFSF_MAX_FACES];
 } gmes_transparent;
 
+/* One probe point (the reference's Probe, gmes/file_io.py:9-48). */
+typedef struct {
+  int32_t comp;   /* field component 0..5 */
+  int32_t pad;
+  int64_t offset; /* linear index into the component's array */
+} gmes_probe;
+
 /* One point source, resolved to one Yee point (gmes/pw_source.py:74-131). */
 typedef struct {
   int32_t comp;   /* field component 0..5 */
@@ -186,6 +193,14 @@ typedef struct gmes_grid_desc {
   int32_t reserved2;
   gmes_transparent* tfsf;
   const struct gmes_grid_desc* incident;
+  /* Probes (optional): after each half's updates and sources, step s of a
+     gmes_step call writes the value of every probe of that half's
+     components to probe_val[s * nprobe + q] (FP64), as FDTD.step writes
+     its E and H recorders (gmes/fdtd.py:1107-1122). */
+  int32_t nprobe;
+  int32_t probe_steps;   /* capacity of probe_val in steps */
+  gmes_probe* probe;
+  double* probe_val;
 } gmes_grid_desc;
 /*
  * State slots (naux) per kind, the same state the reference keeps inside

@@ -7,6 +7,7 @@ bookkeeping.  The tests compare the CPU oracle and the CUDA engine against
 these files; they never need the reference itself.
 
 Usage:  python tests/golden/make_golden.py [case ...]
+        python tests/golden/make_golden.py --probes [case ...]
 """
 
 import json
@@ -61,5 +62,36 @@ def main(names):
         print(f"{name}: init {t1 - t0:.1f}s, {nsteps} steps {t2 - t1:.1f}s", flush=True)
 
 
+# Probe recordings (FDTD.set_probe, gmes/fdtd.py:607-671): the reference's
+# text files for these (case, point) pairs, stored as probe_<case>_<comp>.dat.
+PROBES = {"tfsf2d": (0.2, 0.1, 0.0), "tmz_regression": (0.2, 0.1, 0.0)}
+
+
+def probes(names):
+    import tempfile
+    from oracle.refpkg import load_reference
+    gmes = load_reference()
+    for name in names:
+        if name not in PROBES:
+            continue
+        sim, nsteps = CASES[name](gmes)
+        sim.init()
+        with tempfile.TemporaryDirectory() as tmp:
+            prefix = os.path.join(tmp, "p")
+            sim.set_probe(PROBES[name], prefix)
+            for _ in range(nsteps):
+                sim.step()
+            for rec in sim.e_recorder + sim.h_recorder:
+                rec.close()
+            for f in sorted(os.listdir(tmp)):
+                comp = f[2:4]
+                (HERE / f"probe_{name}_{comp}.dat").write_text(Path(tmp, f).read_text())
+                print("probe", name, comp, flush=True)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1:] or list(CASES))
+    args = sys.argv[1:]
+    if args[:1] == ["--probes"]:
+        probes(args[1:] or list(PROBES))
+    else:
+        main(args or list(CASES))
