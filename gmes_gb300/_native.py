@@ -10,7 +10,7 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libgmes_gb300.so"
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 MAX_CLASSES = 256
 MAX_PML = 4
 MAX_POLES = 8
@@ -18,6 +18,7 @@ MAX_POLES = 8
 FP64, FP32, DF64, FP64_STRICT = 0, 1, 2, 3
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "df64": DF64, "fp64_strict": FP64_STRICT}
 FLAG_DISPERSIVE = 1
+FLAG_COMPLEX = 2
 
 EXPORTS = [
     "gmes_abi_version", "gmes_last_error", "gmes_elem_size", "gmes_field_shape",
@@ -78,7 +79,7 @@ GridDescC._fields_ = [
     ("ntfsf", C.c_int32), ("reserved2", C.c_int32), ("tfsf", C.c_void_p),
     ("incident", C.POINTER(GridDescC)),
     ("nprobe", C.c_int32), ("probe_steps", C.c_int32), ("probe", C.c_void_p),
-    ("probe_val", C.c_void_p),
+    ("probe_val", C.c_void_p), ("bloch_phase", ((C.c_double * 2) * 2) * 6),
 ]
 
 

@@ -85,6 +85,9 @@ gmes_status check_desc(const gmes_grid_desc* g, bool need_buffers) {
   if (need_buffers && g->coef == nullptr) return fail(GMES_ERR_VALUE, "coef is NULL");
   if (need_buffers && g->nsrc > 0 && (g->src == nullptr || g->src_val == nullptr))
     return fail(GMES_ERR_VALUE, "nsrc > 0 but src or src_val is NULL");
+  if ((g->flags & GMES_FLAG_COMPLEX) && g->precision != GMES_FP64 &&
+      g->precision != GMES_FP64_STRICT)
+    return fail(GMES_ERR_VALUE, "complex grids support fp64 and fp64_strict only");
   if (g->ntfsf < 0) return fail(GMES_ERR_VALUE, "ntfsf = %d must be >= 0", g->ntfsf);
   if (g->nprobe < 0 || g->probe_steps < 0)
     return fail(GMES_ERR_VALUE, "negative nprobe / probe_steps");
@@ -99,6 +102,8 @@ gmes_status check_desc(const gmes_grid_desc* g, bool need_buffers) {
     if ((a->active & ((1 << GMES_EX) | (1 << GMES_HY))) != ((1 << GMES_EX) | (1 << GMES_HY)) ||
         a->incident != nullptr || a->ntfsf != 0)
       return fail(GMES_ERR_VALUE, "the incident-field grid must be a plain Ex/Hy grid");
+    if ((a->flags & GMES_FLAG_COMPLEX) != (g->flags & GMES_FLAG_COMPLEX))
+      return fail(GMES_ERR_VALUE, "the incident-field grid must be complex iff the grid is");
   }
   return GMES_OK;
 }
@@ -145,6 +150,7 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
   }
   d.src = g.src;
   d.src_val = g.src_val;
+  std::memcpy(d.phase, g.bloch_phase, sizeof(d.phase));
   if (g.nprobe > 0) {
     d.probe = g.probe;
     d.probe_val = g.probe_val;
@@ -212,6 +218,39 @@ int64_t max_ghost_plane(const GridDev& d) {
   return m;
 }
 
+// The imaginary-plane view of a complex grid: every per-plane pointer moved
+// past its real plane.
+GridDev make_im_view(const GridDev& re, const gmes_grid_desc& g) {
+  GridDev d = re;
+  const int64_t es = elem_size(g.precision);
+  for (int c = 0; c < 6; ++c) {
+    d.f[c] = static_cast<char*>(re.f[c]) + re.npts[c] * es;
+    if (re.aux[c] != nullptr)
+      d.aux[c] = static_cast<char*>(re.aux[c]) + (int64_t)re.naux[c] * re.npts[c] * es;
+  }
+  if (re.src_val != nullptr) d.src_val = re.src_val + (int64_t)g.src_steps * 2 * g.nsrc;
+  for (int k = 0; k < 2; ++k)
+    if (re.tf_field[k] != nullptr)
+      d.tf_field[k] = static_cast<const char*>(re.tf_field[k]) + re.tf_npts[k] * es;
+  if (re.probe_val != nullptr) d.probe_val = re.probe_val + (int64_t)g.probe_steps * g.nprobe;
+  return d;
+}
+
+// Launch plan of a grid and (in *inc) of its TFSF incident-field grid.
+Plan make_plan(const gmes_grid_desc& g, Plan* inc) {
+  Plan p;
+  p.re = make_grid_dev(g);
+  p.cplx = (g.flags & GMES_FLAG_COMPLEX) != 0;
+  p.disp = (g.flags & GMES_FLAG_DISPERSIVE) != 0;
+  p.im = p.cplx ? make_im_view(p.re, g) : p.re;
+  p.incident = nullptr;
+  if (g.ntfsf > 0 && g.incident != nullptr && inc != nullptr) {
+    *inc = make_plan(*g.incident, nullptr);
+    p.incident = inc;
+  }
+  return p;
+}
+
 }  // namespace gmes
 
 using namespace gmes;
@@ -236,18 +275,19 @@ gmes_status gmes_grid_sizes(const gmes_grid_desc* g, int64_t sizes[21]) {
   if (st != GMES_OK) return st;
   if (sizes == nullptr) return fail(GMES_ERR_VALUE, "sizes is NULL");
   const int es = elem_size(g->precision);
+  const int parts = (g->flags & GMES_FLAG_COMPLEX) ? 2 : 1;
   for (int c = 0; c < 6; ++c) {
     int64_t sh[3];
     comp_shape(g->n, g->active, c, sh);
     const int64_t np = sh[0] * sh[1] * sh[2];
     const bool act = (g->active >> c) & 1;
-    sizes[c] = np * es;
+    sizes[c] = np * es * parts;
     sizes[6 + c] = act ? np : 0;
-    sizes[12 + c] = act ? np * es * g->naux[c] : 0;
+    sizes[12 + c] = act ? np * es * g->naux[c] * parts : 0;
   }
   sizes[18] = coef_layout(*g).total;
   sizes[19] = (int64_t)g->nsrc * (int64_t)sizeof(gmes_point_source);
-  sizes[20] = 2 * (int64_t)g->nsrc * (int64_t)sizeof(double);
+  sizes[20] = 2 * (int64_t)g->nsrc * (int64_t)sizeof(double) * parts;
   return GMES_OK;
 }
 
@@ -434,15 +474,9 @@ gmes_status gmes_step(const gmes_grid_desc* g, int32_t nsteps, void* stream) {
     return fail(GMES_ERR_VALUE, "nsteps = %d exceeds the incident grid's source capacity %d",
                 nsteps, g->incident->src_steps);
   if (nsteps == 0) return GMES_OK;
-  const GridDev d = make_grid_dev(*g);
-  cudaError_t e;
-  if (g->ntfsf > 0) {
-    const GridDev a = make_grid_dev(*g->incident);
-    e = launch_step(*g, d, nsteps, static_cast<cudaStream_t>(stream), &a,
-                    (g->incident->flags & GMES_FLAG_DISPERSIVE) != 0);
-  } else {
-    e = launch_step(*g, d, nsteps, static_cast<cudaStream_t>(stream));
-  }
+  Plan inc;
+  const Plan p = make_plan(*g, &inc);
+  cudaError_t e = launch_step(*g, p, nsteps, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching step kernels");
   return GMES_OK;
 }
@@ -461,15 +495,9 @@ gmes_status gmes_half_step(const gmes_grid_desc* g, int32_t side, int32_t step, 
   if (st != GMES_OK) return st;
   if (g->ntfsf > 0 && g->incident->nsrc > 0 && step >= g->incident->src_steps)
     return fail(GMES_ERR_INDEX, "step %d outside the incident grid's source-value buffer", step);
-  const GridDev d = make_grid_dev(*g);
-  cudaError_t e;
-  if (g->ntfsf > 0) {
-    const GridDev a = make_grid_dev(*g->incident);
-    e = launch_half(*g, d, side, step, static_cast<cudaStream_t>(stream), &a,
-                    (g->incident->flags & GMES_FLAG_DISPERSIVE) != 0);
-  } else {
-    e = launch_half(*g, d, side, step, static_cast<cudaStream_t>(stream));
-  }
+  Plan inc;
+  const Plan p = make_plan(*g, &inc);
+  cudaError_t e = launch_half(*g, p, side, step, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching half-step kernels");
   return GMES_OK;
 }
@@ -509,6 +537,8 @@ gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs
     if (st != GMES_OK) return fail(st, "grid %d: %s", q, g_last_error.c_str());
     if (g->ntfsf > 0) return fail(GMES_ERR_VALUE, "grid %d has a TFSF source: not batchable", q);
     if (g->nprobe > 0) return fail(GMES_ERR_VALUE, "grid %d has probes: not batchable", q);
+    if (g->flags & GMES_FLAG_COMPLEX)
+      return fail(GMES_ERR_VALUE, "grid %d is complex: not batchable", q);
     if (precision < 0) precision = g->precision;
     if (g->precision != precision)
       return fail(GMES_ERR_VALUE, "grid %d: all grids of a batch must share one precision", q);
@@ -636,7 +666,7 @@ gmes_status gmes_read_field(const gmes_grid_desc* g, int32_t comp, double* host_
   if (host_out == nullptr) return fail(GMES_ERR_VALUE, "host_out is NULL");
   int64_t sh[3];
   comp_shape(g->n, g->active, comp, sh);
-  const int64_t np = sh[0] * sh[1] * sh[2];
+  const int64_t np = sh[0] * sh[1] * sh[2] * ((g->flags & GMES_FLAG_COMPLEX) ? 2 : 1);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e;
   if (g->precision == GMES_FP64 || g->precision == GMES_FP64_STRICT) {
@@ -666,7 +696,7 @@ gmes_status gmes_write_field(const gmes_grid_desc* g, int32_t comp, const double
   if (host_in == nullptr) return fail(GMES_ERR_VALUE, "host_in is NULL");
   int64_t sh[3];
   comp_shape(g->n, g->active, comp, sh);
-  const int64_t np = sh[0] * sh[1] * sh[2];
+  const int64_t np = sh[0] * sh[1] * sh[2] * ((g->flags & GMES_FLAG_COMPLEX) ? 2 : 1);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e;
   if (g->precision == GMES_FP64 || g->precision == GMES_FP64_STRICT) {
@@ -730,6 +760,8 @@ gmes_status check_tmz(const gmes_grid_desc* g, const gmes_tmz_batch* b, bool nee
     return fail(GMES_ERR_VALUE, "the adjoint path needs a TMz grid (Ez, Hx, Hy; n[2] = 1)");
   if (g->precision == GMES_FP64_STRICT)
     return fail(GMES_ERR_VALUE, "fp64_strict has no adjoint path; use fp64");
+  if (g->flags & GMES_FLAG_COMPLEX)
+    return fail(GMES_ERR_VALUE, "the adjoint path needs a real grid");
   if (b->nbatch < 1 || b->nbatch > 65535)
     return fail(GMES_ERR_VALUE, "nbatch = %d outside [1, 65535]", b->nbatch);
   const int32_t nn[2] = {g->n[0], g->n[1]};
@@ -974,6 +1006,8 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
     if (st != GMES_OK) return st;
     if (g->ntfsf > 0) return fail(GMES_ERR_VALUE, "grid %d has a TFSF source: not batchable", q);
     if (g->nprobe > 0) return fail(GMES_ERR_VALUE, "grid %d has probes: not batchable", q);
+    if (g->flags & GMES_FLAG_COMPLEX)
+      return fail(GMES_ERR_VALUE, "grid %d is complex: not batchable", q);
     if (precision < 0) precision = g->precision;
     if (g->precision != precision)
       return fail(GMES_ERR_VALUE, "grid %d: all grids must share one precision", q);

@@ -159,6 +159,15 @@ struct GridDev {
   double* probe_val;
   int32_t nprobe;
   int32_t pad3;
+  double phase[6][2][2];   // Bloch phase factors (complex grids)
+};
+
+// Host-side launch plan of one grid: its real-plane view, the imaginary-
+// plane view of a complex grid, and the TFSF incident-field grid's plan.
+struct Plan {
+  GridDev re, im;
+  bool cplx, disp;
+  const Plan* incident;
 };
 
 // ---------------------------------------------------------------------------
@@ -321,12 +330,9 @@ cudaError_t launch_tmz_objective(const GridDev& g, const TmzDev& t, int nsteps, 
 GridDev make_grid_dev(const gmes_grid_desc& g);
 
 // Launchers implemented per precision in gmes_step.cu.
-// aux: the incident-field grid of a TFSF source (or null), stepped between
-// the E and H halves of every step.
-cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps,
-                        cudaStream_t s, const GridDev* aux = nullptr, bool aux_disp = false);
-cudaError_t launch_half(const gmes_grid_desc& g, const GridDev& d, int side, int step,
-                        cudaStream_t s, const GridDev* aux = nullptr, bool aux_disp = false);
+cudaError_t launch_step(const gmes_grid_desc& g, const Plan& p, int nsteps, cudaStream_t s);
+cudaError_t launch_half(const gmes_grid_desc& g, const Plan& p, int side, int step,
+                        cudaStream_t s);
 cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nsteps, int blocks,
                          cudaStream_t s);
 cudaError_t launch_raster(const gmes_grid_desc& gd, const GridDev& d, int c,

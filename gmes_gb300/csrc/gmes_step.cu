@@ -523,6 +523,64 @@ __global__ void k_ghost(const GridDev g, int side, int64_t maxplane) {
   ghost_point<T>(g, side, blockIdx.y, t);
 }
 
+// Ghost planes of a complex grid (Bloch boundary, gmes/fdtd.py:811-1097):
+// as ghost_point, but the value is multiplied by the phase factor of each
+// ghost axis in the reference's copy order (own+1, then own+2).  The
+// imaginary plane follows the real plane of every component.  Strict: the
+// product in the fused form numpy's SIMD complex multiply uses,
+// re = fma(pr, vr, -(pi vi)), im = fma(pr, vi, pi vr).
+template <bool STRICT>
+__device__ __forceinline__ void ghost_point_c(const GridDev& g, int side, int item, int64_t t) {
+  const int c = side * 3 + item / 2;
+  if (!(g.active & (1 << c))) return;
+  const int own = c % 3;
+  const int ga = (item & 1) ? (own + 2) % 3 : (own + 1) % 3;
+  const int pa = (ga + 1) % 3, qa = (ga + 2) % 3;
+  const int p_ = pa < qa ? pa : qa, q_ = pa < qa ? qa : pa;
+  const int64_t np = g.sh[c][p_] * g.sh[c][q_];
+  if (t >= np) return;
+  int64_t x[3];
+  x[p_] = t / g.sh[c][q_];
+  x[q_] = t - x[p_] * g.sh[c][q_];
+  x[ga] = side == 0 ? g.sh[c][ga] - 1 : 0;
+  int64_t s[3] = {x[0], x[1], x[2]};
+  bool ghost[2];
+  const int axes[2] = {(own + 1) % 3, (own + 2) % 3};
+  for (int h = 0; h < 2; ++h) {
+    const int ax = axes[h];
+    ghost[h] = side == 0 ? x[ax] == g.sh[c][ax] - 1 : x[ax] == 0;
+    if (ghost[h]) s[ax] = side == 0 ? 0 : g.sh[c][ax] - 1;
+  }
+  double* fr = static_cast<double*>(g.f[c]);
+  double* fi = fr + g.npts[c];
+  const int64_t dst = x[0] * g.st[c][0] + x[1] * g.st[c][1] + x[2];
+  const int64_t src = s[0] * g.st[c][0] + s[1] * g.st[c][1] + s[2];
+  double vr = fr[src], vi = fi[src];
+  for (int h = 0; h < 2; ++h) {
+    if (!ghost[h]) continue;
+    const double pr = g.phase[c][h][0], pi = g.phase[c][h][1];
+    double nr, ni;
+    if (STRICT) {
+      nr = __fma_rn(pr, vr, -__dmul_rn(pi, vi));
+      ni = __fma_rn(pr, vi, __dmul_rn(pi, vr));
+    } else {
+      nr = pr * vr - pi * vi;
+      ni = pr * vi + pi * vr;
+    }
+    vr = nr;
+    vi = ni;
+  }
+  fr[dst] = vr;
+  fi[dst] = vi;
+}
+
+template <bool STRICT>
+__global__ void k_ghost_c(const GridDev g, int side, int64_t maxplane) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= maxplane) return;
+  ghost_point_c<STRICT>(g, side, blockIdx.y, t);
+}
+
 // Point sources of one half-step (gmes/pw_source.py:74-131), applied after
 // that half's material update.  `v` has been computed on the host in FP64.
 template <class P, bool STRICT>
@@ -675,17 +733,18 @@ __global__ void k_multi_sources(const BatchView v, int side, int s) {
 }
 
 template <class P, bool STRICT>
-cudaError_t run_steps(const GridDev& d, int nsteps, int side_mask, int st0, cudaStream_t s,
-                      bool disp, const GridDev* aux = nullptr, bool aux_disp = false);
+cudaError_t run_steps(const Plan& p, int nsteps, int side_mask, int st0, cudaStream_t s);
 
 // One half-step: ghost copy of the other half's components, the fused
-// update of this half's components, this half's point sources and TFSF
-// corrections; after the E half, one full step of the TFSF incident-field
-// grid (FDTD.step's _step_aux_fdtd, gmes/fdtd.py:1113).
+// update of this half's components, this half's point sources, TFSF
+// corrections and probes; after the E half, one full step of the TFSF
+// incident-field grid (FDTD.step's _step_aux_fdtd, gmes/fdtd.py:1113).
+// A complex grid runs every per-plane kernel on its real and imaginary
+// planes; only the ghost copy couples them.
 template <class P, bool STRICT>
-void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp,
-              const GridDev* aux, bool aux_disp) {
+void run_half(const Plan& p, int side, int st, cudaStream_t s) {
   using T = typename P::T;
+  const GridDev& d = p.re;
   int64_t maxplane = 1;
   for (int c = 0; c < 6; ++c)
     for (int a = 0; a < 3; ++a)
@@ -695,55 +754,56 @@ void run_half(const GridDev& d, int side, int st, cudaStream_t s, bool disp,
       }
   const dim3 ggrid((unsigned)((maxplane + 255) / 256), 6);
   constexpr int kMaxY = 65535;
-  k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
+  if (p.cplx)
+    k_ghost_c<STRICT><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
+  else
+    k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
   int bx_log2 = 0;
   while (bx_log2 < 5 && (1 << bx_log2) < d.n[2]) ++bx_log2;
   const int bx = 1 << bx_log2, by = kThreads / bx;
-  for (int i0 = 0; i0 < d.n[0]; i0 += kMaxY) {
-    const dim3 grid((unsigned)((d.n[2] + bx - 1) / bx), (unsigned)((d.n[1] + by - 1) / by),
-                    (unsigned)min(kMaxY, d.n[0] - i0));
-    // Measured on GB300: a compile-time active mask (all six components) or
-    // 32-bit offsets do not speed this kernel up -- the full-mask variant
-    // ran ~35% slower at 256^3 -- so one runtime-mask, 64-bit-offset
-    // instantiation serves every grid.
-    launch_cell<P, STRICT, 0, int64_t>(d, side, disp, grid, bx_log2, i0, s);
+  const int nplanes = p.cplx ? 2 : 1;
+  for (int part = 0; part < nplanes; ++part) {
+    const GridDev& v = part == 0 ? p.re : p.im;
+    for (int i0 = 0; i0 < d.n[0]; i0 += kMaxY) {
+      const dim3 grid((unsigned)((d.n[2] + bx - 1) / bx), (unsigned)((d.n[1] + by - 1) / by),
+                      (unsigned)min(kMaxY, d.n[0] - i0));
+      // Measured on GB300: a compile-time active mask (all six components) or
+      // 32-bit offsets do not speed this kernel up -- the full-mask variant
+      // ran ~35% slower at 256^3 -- so one runtime-mask, 64-bit-offset
+      // instantiation serves every grid.
+      launch_cell<P, STRICT, 0, int64_t>(v, side, p.disp, grid, bx_log2, i0, s);
+    }
   }
-  if (d.nsrc > 0)
-    k_sources<P, STRICT><<<(d.nsrc + 127) / 128, 128, 0, s>>>(d, side, 2 * (int64_t)st + side);
-  if (d.ntfsf > 0) k_transparent<P, STRICT><<<(d.ntfsf + 127) / 128, 128, 0, s>>>(d, side);
-  if (d.nprobe > 0) k_probes<P><<<(d.nprobe + 127) / 128, 128, 0, s>>>(d, side, st);
-  if (side == 0 && aux != nullptr) run_steps<P, STRICT>(*aux, 1, 3, st, s, aux_disp);
+  for (int part = 0; part < nplanes; ++part) {
+    const GridDev& v = part == 0 ? p.re : p.im;
+    if (v.nsrc > 0)
+      k_sources<P, STRICT><<<(v.nsrc + 127) / 128, 128, 0, s>>>(v, side, 2 * (int64_t)st + side);
+    if (v.ntfsf > 0) k_transparent<P, STRICT><<<(v.ntfsf + 127) / 128, 128, 0, s>>>(v, side);
+    if (v.nprobe > 0) k_probes<P><<<(v.nprobe + 127) / 128, 128, 0, s>>>(v, side, st);
+  }
+  if (side == 0 && p.incident != nullptr) run_steps<P, STRICT>(*p.incident, 1, 3, st, s);
 }
 
 template <class P, bool STRICT>
-cudaError_t run_steps(const GridDev& d, int nsteps, int side_mask, int st0, cudaStream_t s,
-                      bool disp, const GridDev* aux, bool aux_disp) {
+cudaError_t run_steps(const Plan& p, int nsteps, int side_mask, int st0, cudaStream_t s) {
   for (int st = 0; st < nsteps; ++st) {
-    if (side_mask & 1) run_half<P, STRICT>(d, 0, st0 + st, s, disp, aux, aux_disp);
-    if (side_mask & 2) run_half<P, STRICT>(d, 1, st0 + st, s, disp, aux, aux_disp);
+    if (side_mask & 1) run_half<P, STRICT>(p, 0, st0 + st, s);
+    if (side_mask & 2) run_half<P, STRICT>(p, 1, st0 + st, s);
   }
   return cudaGetLastError();
 }
 
-template <class P, bool STRICT>
-cudaError_t dispatch(const gmes_grid_desc& g, const GridDev& d, int nsteps, int side_mask,
-                     int st0, cudaStream_t s, const GridDev* aux, bool aux_disp) {
-  const bool disp = (g.flags & GMES_FLAG_DISPERSIVE) != 0;
-  return run_steps<P, STRICT>(d, nsteps, side_mask, st0, s, disp, aux, aux_disp);
-}
-
-cudaError_t dispatch_precision(const gmes_grid_desc& g, const GridDev& d, int nsteps,
-                               int side_mask, int st0, cudaStream_t s, const GridDev* aux,
-                               bool aux_disp) {
+cudaError_t dispatch_precision(const gmes_grid_desc& g, const Plan& p, int nsteps,
+                               int side_mask, int st0, cudaStream_t s) {
   switch (g.precision) {
     case GMES_FP64:
-      return dispatch<PolF64, false>(g, d, nsteps, side_mask, st0, s, aux, aux_disp);
+      return run_steps<PolF64, false>(p, nsteps, side_mask, st0, s);
     case GMES_FP64_STRICT:
-      return dispatch<PolF64, true>(g, d, nsteps, side_mask, st0, s, aux, aux_disp);
+      return run_steps<PolF64, true>(p, nsteps, side_mask, st0, s);
     case GMES_FP32:
-      return dispatch<PolF32, false>(g, d, nsteps, side_mask, st0, s, aux, aux_disp);
+      return run_steps<PolF32, false>(p, nsteps, side_mask, st0, s);
     case GMES_DF64:
-      return dispatch<PolDF, false>(g, d, nsteps, side_mask, st0, s, aux, aux_disp);
+      return run_steps<PolDF, false>(p, nsteps, side_mask, st0, s);
     default:
       return cudaErrorInvalidValue;
   }
@@ -792,14 +852,13 @@ cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nstep
   }
 }
 
-cudaError_t launch_step(const gmes_grid_desc& g, const GridDev& d, int nsteps, cudaStream_t s,
-                        const GridDev* aux, bool aux_disp) {
-  return dispatch_precision(g, d, nsteps, 3, 0, s, aux, aux_disp);
+cudaError_t launch_step(const gmes_grid_desc& g, const Plan& p, int nsteps, cudaStream_t s) {
+  return dispatch_precision(g, p, nsteps, 3, 0, s);
 }
 
-cudaError_t launch_half(const gmes_grid_desc& g, const GridDev& d, int side, int step,
-                        cudaStream_t s, const GridDev* aux, bool aux_disp) {
-  return dispatch_precision(g, d, 1, side == 0 ? 1 : 2, step, s, aux, aux_disp);
+cudaError_t launch_half(const gmes_grid_desc& g, const Plan& p, int side, int step,
+                        cudaStream_t s) {
+  return dispatch_precision(g, p, 1, side == 0 ? 1 : 2, step, s);
 }
 
 }  // namespace gmes

@@ -65,6 +65,15 @@ class GridEngine:
         d.nparam = len(pool)
         d.src_steps = self.src_chunk
         d.flags = N.FLAG_DISPERSIVE if scene.dispersive else 0
+        self.cmplx = bool(scene.cmplx)
+        if self.cmplx:
+            if self.prec not in (N.FP64, N.FP64_STRICT):
+                raise ValueError("complex (Bloch) fields need precision fp64 or fp64_strict")
+            d.flags |= N.FLAG_COMPLEX
+            for c in range(6):
+                for h in range(2):
+                    d.bloch_phase[c][h][0] = float(scene.bloch_phase[c, h, 0])
+                    d.bloch_phase[c][h][1] = float(scene.bloch_phase[c, h, 1])
         sizes = (C.c_int64 * 21)()
         N.check(self.lib.gmes_grid_sizes(C.byref(d), sizes))
         self.sizes = list(sizes)
@@ -74,7 +83,9 @@ class GridEngine:
         self.cls = []
         for c in range(6):
             shape = scene.shape(c)
-            if self.prec in (N.FP64, N.FP64_STRICT):
+            if self.cmplx:
+                t = torch.zeros((2,) + shape, dtype=torch.float64, device=dev)  # re, im planes
+            elif self.prec in (N.FP64, N.FP64_STRICT):
                 t = torch.zeros(shape, dtype=torch.float64, device=dev)
             elif self.prec == N.FP32:
                 t = torch.zeros(shape, dtype=torch.float32, device=dev)
@@ -105,7 +116,8 @@ class GridEngine:
             arr = (N.PointSourceC * len(srcs))(*[N.PointSourceC(c, m, o) for c, m, o in srcs])
             host = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8)
             self.src = host.to(dev)
-            self.src_val = torch.zeros((self.src_chunk, 2, len(srcs)), dtype=torch.float64,
+            lead = (2,) if self.cmplx else ()
+            self.src_val = torch.zeros(lead + (self.src_chunk, 2, len(srcs)), dtype=torch.float64,
                                        device=dev)
             self.src_host = torch.zeros(self.src_val.shape, dtype=torch.float64).pin_memory()
             d.src = self.src.data_ptr()
@@ -280,8 +292,9 @@ class GridEngine:
             arr = (N.ProbeC * len(points))(*[N.ProbeC(c, 0, o) for c, o in points])
             self.probes = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(
                 self.device)
-            self.probe_val = torch.zeros((self.src_chunk, len(points)), dtype=torch.float64,
-                                         device=self.device)
+            lead = (2,) if self.cmplx else ()
+            self.probe_val = torch.zeros(lead + (self.src_chunk, len(points)),
+                                         dtype=torch.float64, device=self.device)
             d.nprobe = len(points)
             d.probe_steps = self.src_chunk
             d.probe = self.probes.data_ptr()
@@ -294,6 +307,9 @@ class GridEngine:
     def probe_values(self, k):
         """(k, nprobe) float64 numpy: the probes of the last k recorded steps of a chunk."""
         self._stream.synchronize()
+        if self.cmplx:
+            v = self.probe_val[:, :k].cpu().numpy()
+            return v[0] + 1j * v[1]
         return self.probe_val[:k].cpu().numpy()
 
     # -- stepping ----------------------------------------------------------
@@ -320,9 +336,17 @@ class GridEngine:
         # chunk's asynchronous copy
         if self._staged is not None:
             self._staged.synchronize()
-        self.src_host[:k].copy_(torch.from_numpy(np.ascontiguousarray(vals)))
+        vals = np.asarray(vals)
+        if self.cmplx:
+            self.src_host[0, :k].copy_(torch.from_numpy(np.ascontiguousarray(vals.real)))
+            self.src_host[1, :k].copy_(torch.from_numpy(np.ascontiguousarray(vals.imag)))
+        else:
+            self.src_host[:k].copy_(torch.from_numpy(np.ascontiguousarray(vals)))
         with torch.cuda.stream(stream):
-            self.src_val[:k].copy_(self.src_host[:k], non_blocking=True)
+            if self.cmplx:
+                self.src_val[:, :k].copy_(self.src_host[:, :k], non_blocking=True)
+            else:
+                self.src_val[:k].copy_(self.src_host[:k], non_blocking=True)
             self._staged = torch.cuda.Event()
             self._staged.record(stream)
 
@@ -381,15 +405,20 @@ class GridEngine:
         return self.fields[c]
 
     def read(self, c):
-        """Component ``c`` as a float64 numpy array."""
+        """Component ``c`` as a float64 (complex128 for complex grids) numpy array."""
         t = self.fields[c]
+        if self.cmplx:
+            a = t.cpu().numpy()
+            return a[0] + 1j * a[1]
         if self.prec == N.DF64:
             return (t[..., 0].double() + t[..., 1].double()).cpu().numpy()
         return t.double().cpu().numpy()
 
     def read_tensor(self, c):
-        """Component ``c`` as a float64 device tensor."""
+        """Component ``c`` as a float64 (complex128) device tensor."""
         t = self.fields[c]
+        if self.cmplx:
+            return _torch().complex(t[0], t[1])
         if self.prec == N.DF64:
             return t[..., 0].double() + t[..., 1].double()
         return t.double()
@@ -397,6 +426,11 @@ class GridEngine:
     def write(self, c, key, value):
         torch = _torch()
         t = self.fields[c]
+        if self.cmplx:
+            v = torch.as_tensor(np.asarray(value, np.complex128), device=self.device)
+            t[0][key] = v.real
+            t[1][key] = v.imag
+            return
         if self.prec == N.DF64:
             v = torch.as_tensor(value, dtype=torch.float64, device=self.device)
             hi = v.float()
@@ -408,8 +442,13 @@ class GridEngine:
 
     def write_all(self, c, array):
         torch = _torch()
-        a = torch.as_tensor(np.ascontiguousarray(array, dtype=np.float64), device=self.device)
         t = self.fields[c]
+        if self.cmplx:
+            a = np.asarray(array, np.complex128)
+            t[0].copy_(torch.as_tensor(np.ascontiguousarray(a.real), device=self.device))
+            t[1].copy_(torch.as_tensor(np.ascontiguousarray(a.imag), device=self.device))
+            return
+        a = torch.as_tensor(np.ascontiguousarray(array, dtype=np.float64), device=self.device)
         if self.prec == N.DF64:
             hi = a.float()
             t[..., 0] = hi
@@ -425,6 +464,8 @@ class GridEngine:
         torch = _torch()
         shape = self.scene.shape(c)
         na = self.desc.naux[c]
+        if self.cmplx:
+            return a.view(torch.float64).view((2, na) + shape)
         if self.prec in (N.FP64, N.FP64_STRICT):
             return a.view(torch.float64).view((na,) + shape)
         if self.prec == N.FP32:

@@ -72,7 +72,7 @@ class FieldView:
 
     @property
     def dtype(self):
-        return np.dtype(np.float64)
+        return np.dtype(np.complex128 if self._sim.cmplx else np.float64)
 
     @property
     def size(self):
@@ -135,10 +135,14 @@ class FDTD:
         self.space = space
         self.dx, self.dy, self.dz = self.space.dr
         self.precision = precision
-        if bloch is not None:
-            raise NotImplementedError("Bloch (complex) fields are not implemented yet")
-        self.cmplx = False
-        self.bloch = None
+        if bloch is None:
+            self.cmplx = False
+            self.bloch = None
+        else:
+            # complex fields; the ghost copies carry the Bloch phase
+            # (gmes/fdtd.py:179-208, 811-1097)
+            self.cmplx = True
+            self.bloch = np.array(bloch, np.double)
         default_medium = next(i for i in geom_list if isinstance(i, DefaultMedium))
         dt_limit = self._dt_limit(space, default_medium.material.eps_inf,
                                   default_medium.material.mu_inf)
@@ -154,6 +158,14 @@ class FDTD:
             self.space.display_info()
             print("dt:", time_step_size)
             print("courant ratio:", self.courant_ratio)
+            if self.cmplx:
+                # the numerical Bloch wave vector (Taflove & Hagness eq. 4.14a)
+                ds = np.array(self.space.dr)
+                mat = default_medium.material
+                S = 1 / sqrt(mat.eps_inf * mat.mu_inf) * time_step_size / ds
+                print("Bloch wave vector is", self.bloch)
+                print("numerical Bloch wave vector is",
+                      2 * sqrt(mat.eps_inf) / ds * np.arcsin(np.sin(self.bloch * S * ds / 2) / S))
         self.geom_list = geom_list
         for go in self.geom_list:
             go.init(self.space)
@@ -196,7 +208,7 @@ class FDTD:
         if self._scene is None:
             self._scene = compile_scene(self.space, self.geom_list, self.e_field_compnt,
                                         self.h_field_compnt, self.src_list, self.geom_tree,
-                                        self.time_step.dt)
+                                        self.time_step.dt, bloch=self.bloch)
         return self._scene
 
     def init(self):
@@ -345,6 +357,7 @@ class FDTD:
                              geom_list=deepcopy(self.geom_list, memo),
                              src_list=deepcopy(self.src_list, memo),
                              courant_ratio=self.courant_ratio, dt=self.time_step.dt,
+                             bloch=deepcopy(self.bloch, memo),
                              verbose=self.verbose, precision=self.precision)
         memo[id(self)] = new
         if self._engine is not None:
@@ -377,7 +390,8 @@ class _Probe:
         self.f.write("# dt=" + str(dt) + "\n")
 
     def write(self, n, value):
-        self.f.write(str(n) + " " + str(np.float64(value)) + "\n")
+        v = np.complex128(value) if np.iscomplexobj(value) else np.float64(value)
+        self.f.write(str(n) + " " + str(v) + "\n")
 
     def close(self):
         if not self.f.closed:

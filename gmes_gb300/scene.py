@@ -62,6 +62,8 @@ class Scene:
         self.pmls = []
         self.sources = []
         self.tfsf = None      # (incident Scene, [(comp, offset, faces)]) of a TFSF source
+        self.cmplx = False    # complex fields with Bloch phases
+        self.bloch_phase = np.zeros((6, 2, 2))
         self.shapes = None
         self._geom = None
         self._space = None
@@ -163,7 +165,29 @@ def _class_table(geom_list, comp, scene):
     return descs, lut
 
 
-def compile_scene(space, geom_list, e_comps, h_comps, src_list, geom_tree, dt):
+def bloch_phases(space, scene, bloch):
+    """Phase factor of each ghost copy (gmes/fdtd.py:811-1097): the E ghost
+    plane (last) along axis a receives exp(1j k_a (x_last - x_0)) times plane
+    0, the H ghost plane (0) exp(1j k_a (x_0 - x_last)) times the last plane;
+    rows (component, h) with h = 0 for axis own+1 and 1 for own+2."""
+    from cmath import exp as cexp
+    ph = np.zeros((6, 2, 2))
+    for comp in scene.active:
+        c = comp.index
+        own = c % 3
+        sh = scene.shape(c)
+        for h, a in enumerate(((own + 1) % 3, (own + 2) % 3)):
+            last = [0, 0, 0]
+            last[a] = sh[a] - 1
+            x0 = space.index_to_space(comp, 0, 0, 0)[a]
+            xl = space.index_to_space(comp, *last)[a]
+            dest, src = (xl, x0) if c < 3 else (x0, xl)
+            p = cexp(1j * bloch[a] * (dest - src))
+            ph[c, h] = (p.real, p.imag)
+    return ph
+
+
+def compile_scene(space, geom_list, e_comps, h_comps, src_list, geom_tree, dt, bloch=None):
     """Class tables, rasteriser records and point sources of a scene.
 
     No per-point work happens here: the class maps are built on the GPU by
@@ -173,6 +197,9 @@ def compile_scene(space, geom_list, e_comps, h_comps, src_list, geom_tree, dt):
     scene = Scene(space.whole_field_size, active, space.dr, space.half_size, dt)
     scene._geom = list(geom_list)
     scene._space = space
+    if bloch is not None:
+        scene.cmplx = True
+        scene.bloch_phase = bloch_phases(space, scene, bloch)
     for comp in active:
         descs, lut = _class_table(geom_list, comp, scene)
         scene.classes[comp.index] = descs
@@ -243,12 +270,13 @@ def class_arrays(scene):
 def source_values(scene, dt, n0, nsteps):
     """Source values for steps whose first E half-step is at time step n0 + 0.5.
 
-    Returns float64 array (nsteps, 2, nsrc): [s, 0] at n = n0 + s + 0.5 (E
+    Returns (nsteps, 2, nsrc) float64 (complex128 for a complex scene):
+    [s, 0] at n = n0 + s + 0.5 (E
     half), [s, 1] at n = n0 + s + 1 (H half), matching TimeStep.half_step_up
     (gmes/fdtd.py:47-50) and the time tag dt * n of gmes/pw_source.py:80.
     """
     ns = len(scene.sources)
-    out = np.zeros((nsteps, 2, ns), np.float64)
+    out = np.zeros((nsteps, 2, ns), np.complex128 if scene.cmplx else np.float64)
     n = float(n0)
     for s in range(nsteps):
         n += 0.5

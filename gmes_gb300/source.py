@@ -197,7 +197,7 @@ class TotalFieldScatteredField(Src):
         from .tfsf import incident_grid
         self.geom_tree = geom_tree
         self.src_time.init(cmplx)
-        self.aux_fdtd = incident_grid(self, space, geom_tree)
+        self.aux_fdtd = incident_grid(self, space, geom_tree, cmplx)
 
     def display_info(self, indent=0):
         print(" " * indent, "plane-wave source:")

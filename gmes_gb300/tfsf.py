@@ -107,7 +107,7 @@ def dispersion_1d(ds, zeta, v, omega, dt, k):
     return lhs - rhs
 
 
-def incident_grid(src, space, geom_tree):
+def incident_grid(src, space, geom_tree, cmplx=False):
     """The TEMz incident-field simulation of a TFSF source (gmes/source.py:579-651)."""
     from copy import deepcopy
     from .fdtd import TEMzFDTD
@@ -136,7 +136,8 @@ def incident_grid(src, space, geom_tree):
     geom = (DefaultMedium(material=material), Shell(material=Cpml(), thickness=pml))
     sources = (PointSource(src_time=deepcopy(src.src_time), component=const.Ex,
                            center=(0, 0, -max_dist - delta)),)
-    return TEMzFDTD(aux_space, list(geom), list(sources), dt=space.dt, verbose=False)
+    return TEMzFDTD(aux_space, list(geom), list(sources), dt=space.dt,
+                    bloch=(0, 0, 0) if cmplx else None, verbose=False)
 
 
 def _coords(space, comp, axis, idx):

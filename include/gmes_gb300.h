@@ -46,7 +46,7 @@
 extern "C" {
 #endif
 
-#define GMES_ABI_VERSION 3
+#define GMES_ABI_VERSION 4
 #define GMES_MAX_CLASSES 256 /* class ids are u8 */
 #define GMES_MAX_PML 4       /* PML materials per grid */
 #define GMES_MAX_POLES 8     /* Drude/Lorentz poles, DCP terms per class */
@@ -80,6 +80,14 @@ typedef enum {
 
 /* gmes_grid_desc.flags */
 #define GMES_FLAG_DISPERSIVE 1 /* some E class is DRUDE, LORENTZ or DCP */
+/* Complex fields (the reference's Cmplx updaters with a Bloch boundary,
+   src/pw_material.i:387, gmes/fdtd.py:811-1097).  Every field, state,
+   source-value and probe buffer holds its real plane followed by its
+   imaginary plane (twice gmes_grid_sizes' real size); the update
+   coefficients are real, so the two planes are updated independently and
+   couple only through the Bloch phases of the ghost copies.  FP64 and
+   FP64_STRICT only. */
+#define GMES_FLAG_COMPLEX 2
 
 /* Field components: bit c of gmes_grid_desc.active. */
 enum { GMES_EX = 0, GMES_EY = 1, GMES_EZ = 2, GMES_HX = 3, GMES_HY = 4, GMES_HZ = 5 };
@@ -201,6 +209,11 @@ typedef struct gmes_grid_desc {
   int32_t probe_steps;   /* capacity of probe_val in steps */
   gmes_probe* probe;
   double* probe_val;
+  /* Complex grids: the ghost plane along the h-th curl axis (h = 0: own+1,
+     h = 1: own+2) of component c receives bloch_phase[c][h] = (re, im)
+     times its source plane, the two axes in that order (corners get both
+     factors); the reference's exp(1j k_a (x_dest - x_src)). */
+  double bloch_phase[6][2][2];
 } gmes_grid_desc;
 /*
  * State slots (naux) per kind, the same state the reference keeps inside
@@ -222,6 +235,7 @@ gmes_status gmes_field_shape(const gmes_grid_desc* g, int32_t comp, int64_t shap
  *   sizes[0..5]   field[c]        sizes[6..11]  cls[c]
  *   sizes[12..17] aux[c]          sizes[18]     coef
  *   sizes[19]     src             sizes[20]     src_val for one step
+ * (complex grids: field, aux and src_val sizes include both planes)
  */
 gmes_status gmes_grid_sizes(const gmes_grid_desc* g, int64_t sizes[21]);
 

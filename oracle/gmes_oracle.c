@@ -97,6 +97,10 @@ typedef struct oracle_s {
   double* tf_r0;
   double* tf_r1;
   int64_t* tf_sample;
+  /* complex grids: this oracle holds the real parts, `imag` the imaginary
+     parts; the ghost copies multiply by the Bloch phases */
+  struct oracle_s* imag;
+  double phase[6][2][2];
 } oracle;
 
 static void comp_shape(const int n[3], int active, int c, int64_t sh[3]) {
@@ -683,6 +687,83 @@ int oracle_step_tfsf(oracle* o, int nsteps, const double* src_vals, const double
 
 int oracle_step(oracle* o, int nsteps, const double* src_vals) {
   return oracle_step_tfsf(o, nsteps, src_vals, NULL);
+}
+
+/* ---- complex fields (Bloch boundary) --------------------------------------
+ * The update coefficients are real (src/pw_*.hh keep them double for T =
+ * complex<double>), so the real and imaginary parts evolve independently
+ * except in the ghost copies, which multiply the source plane by the Bloch
+ * phase exp(1j k_a (x_dest - x_src)) (gmes/fdtd.py:811-1097), the two
+ * curl axes in order.  The reference forms phase * plane with numpy's
+ * complex multiply, which (SIMD build, x86-64 with AVX-512 where the golden
+ * vectors were made) evaluates re = fma(pr, vr, -(pi vi)),
+ * im = fma(pr, vi, pi vr); the same fused form is used here. */
+static void chatter_complex(oracle* re, oracle* im, int c) {
+  if (!(re->active & (1 << c))) return;
+  const int own = c % 3;
+  const int ax[2] = {(own + 1) % 3, (own + 2) % 3};
+  const int64_t* sh = re->sh[c];
+  for (int h = 0; h < 2; ++h) {
+    const int axis = ax[h];
+    const int64_t last = sh[axis] - 1;
+    const int64_t dst = c < 3 ? last : 0, src = c < 3 ? 0 : last;
+    const double pr = re->phase[c][h][0], pi = re->phase[c][h][1];
+    const int p = (axis + 1) % 3, q = (axis + 2) % 3;
+    for (int64_t u = 0; u < sh[p]; ++u)
+      for (int64_t v = 0; v < sh[q]; ++v) {
+        int64_t x[3], y[3];
+        x[axis] = dst; x[p] = u; x[q] = v;
+        y[axis] = src; y[p] = u; y[q] = v;
+        const int64_t xo = (x[0] * sh[1] + x[1]) * sh[2] + x[2];
+        const int64_t yo = (y[0] * sh[1] + y[1]) * sh[2] + y[2];
+        const double vr = re->f[c][yo], vi = im->f[c][yo];
+        re->f[c][xo] = fma(pr, vr, -(pi * vi));
+        im->f[c][xo] = fma(pr, vi, pi * vr);
+      }
+  }
+}
+
+int oracle_set_complex(oracle* re, oracle* im, const double* phase) {
+  re->imag = im;
+  memcpy(re->phase, phase, sizeof(re->phase));
+  return 0;
+}
+
+/* vals_re / vals_im: [nsteps][2][nsrc] real and imaginary source values;
+   aux_re / aux_im the same for the TFSF incident-field grid (a complex
+   pair itself), or NULL. */
+int oracle_step_complex(oracle* re, int nsteps, const double* vals_re, const double* vals_im,
+                        const double* aux_re, const double* aux_im) {
+  oracle* im = re->imag;
+  if (!im) return -1;
+  if (re->incident && (!aux_re || !aux_im || !re->incident->imag)) return -1;
+  for (int s = 0; s < nsteps; ++s) {
+    for (int c = 3; c < 6; ++c) chatter_complex(re, im, c);
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < re->nupd[c]; ++k) {
+        run_updater(re, &re->upd[c][k]);
+        run_updater(im, &im->upd[c][k]);
+      }
+    apply_sources(re, 0, vals_re + (int64_t)(2 * s) * re->nsrc);
+    apply_sources(im, 0, vals_im + (int64_t)(2 * s) * im->nsrc);
+    apply_transparent(re, 0);
+    apply_transparent(im, 0);
+    if (re->incident) {
+      const int64_t na = (int64_t)(2 * s) * re->incident->nsrc;
+      oracle_step_complex(re->incident, 1, aux_re + na, aux_im + na, NULL, NULL);
+    }
+    for (int c = 0; c < 3; ++c) chatter_complex(re, im, c);
+    for (int c = 3; c < 6; ++c)
+      for (int k = 0; k < re->nupd[c]; ++k) {
+        run_updater(re, &re->upd[c][k]);
+        run_updater(im, &im->upd[c][k]);
+      }
+    apply_sources(re, 1, vals_re + (int64_t)(2 * s + 1) * re->nsrc);
+    apply_sources(im, 1, vals_im + (int64_t)(2 * s + 1) * im->nsrc);
+    apply_transparent(re, 1);
+    apply_transparent(im, 1);
+  }
+  return 0;
 }
 
 /* ---- reset and per-point permittivity ------------------------------------ */

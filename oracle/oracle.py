@@ -79,6 +79,11 @@ def load():
                                    P(C.c_int64), C.c_int, P(C.c_int), P(C.c_int64),
                                    P(C.c_double), P(C.c_double)]
     lib.oracle_destroy.argtypes = [C.c_void_p]
+    lib.oracle_set_complex.restype = C.c_int
+    lib.oracle_set_complex.argtypes = [C.c_void_p, C.c_void_p, P(C.c_double)]
+    lib.oracle_step_complex.restype = C.c_int
+    lib.oracle_step_complex.argtypes = [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double),
+                                        P(C.c_double), P(C.c_double)]
     _lib = lib
     return lib
 
@@ -88,22 +93,38 @@ def _dp(a):
 
 
 class Oracle:
-    """CPU FDTD run of a compiled Scene (FP64, reference operation order)."""
+    """CPU FDTD run of a compiled Scene (FP64, reference operation order).
+
+    A complex (Bloch) scene runs as two C oracles, real and imaginary parts,
+    coupled by the phase-shifted ghost copies (oracle_step_complex)."""
 
     def __init__(self, scene):
-        from gmes_gb300.scene import class_arrays, source_offsets
         self.lib = load()
         self.scene = scene
+        self.cmplx = bool(getattr(scene, "cmplx", False))
+        self.incident = Oracle(scene.tfsf[0]) if scene.tfsf is not None else None
+        self.h = self._make(self.incident.h if self.incident is not None else None)
+        self.h_im = None
+        if self.cmplx:
+            self.h_im = self._make(self.incident.h_im if self.incident is not None else None)
+            ph = np.ascontiguousarray(scene.bloch_phase, np.float64)
+            self.lib.oracle_set_complex(self.h, self.h_im, _dp(ph))
+        self.n = 0.0
+
+    def _make(self, incident_handle):
+        """One C oracle with the scene's classes, maps, sources and TFSF table."""
+        from gmes_gb300.scene import class_arrays, source_offsets
+        scene = self.scene
         n = (C.c_int * 3)(*scene.n)
         dr = (C.c_double * 3)(*scene.dr)
         half = (C.c_double * 3)(*scene.half)
-        self.h = self.lib.oracle_create(n, scene.active_mask, dr, half, scene.dt)
-        if not self.h:
+        h = self.lib.oracle_create(n, scene.active_mask, dr, half, scene.dt)
+        if not h:
             raise MemoryError("oracle allocation failed")
         rows, pool, pmls = class_arrays(scene)
         for p in pmls:
             r = self.lib.oracle_add_pml(
-                self.h, p["kind"], (C.c_double * 3)(*p["sigma_max"]), p["m"], p["kappa_max"],
+                h, p["kind"], (C.c_double * 3)(*p["sigma_max"]), p["m"], p["kappa_max"],
                 p["m_a"], p["a_max"], p["d"], (C.c_double * 3)(*p["center"]),
                 (C.c_double * 3)(*p["half_size"]))
             if r < 0:
@@ -114,25 +135,23 @@ class Oracle:
             for _ in scene.classes[c]:
                 r = rows[k]
                 prm = np.ascontiguousarray(pool[r["param_off"]:r["param_off"] + r["nparam"]])
-                if self.lib.oracle_add_class(self.h, c, r["kind"], r["eps"], r["pml"], r["npole"],
+                if self.lib.oracle_add_class(h, c, r["kind"], r["eps"], r["pml"], r["npole"],
                                              r["ncp"], _dp(prm), r["nparam"]) < 0:
                     raise ValueError("bad class")
                 k += 1
         for c in range(6):
             if (scene.active_mask >> c) & 1:
                 m = np.ascontiguousarray(scene.host_cls(c), np.uint8)
-                if self.lib.oracle_set_class_map(self.h, c,
+                if self.lib.oracle_set_class_map(h, c,
                                                  m.ctypes.data_as(C.POINTER(C.c_uint8))) != 0:
                     raise ValueError("bad class map")
         srcs = source_offsets(scene)
         comp = (C.c_int * max(1, len(srcs)))(*[s[0] for s in srcs])
         mode = (C.c_int * max(1, len(srcs)))(*[s[1] for s in srcs])
         off = (C.c_int64 * max(1, len(srcs)))(*[s[2] for s in srcs])
-        self.lib.oracle_set_sources(self.h, len(srcs), comp, mode, off)
-        self.incident = None
+        self.lib.oracle_set_sources(h, len(srcs), comp, mode, off)
         if scene.tfsf is not None:
-            aux_scene, points = scene.tfsf
-            self.incident = Oracle(aux_scene)
+            points = scene.tfsf[1]
             n = len(points)
             tc = np.zeros(n, np.int32)
             nf = np.zeros(n, np.int32)
@@ -147,40 +166,62 @@ class Oracle:
                     coef[q, k], r0[q, k], r1[q, k], smp[q, k] = cf, a, b, sp
             ip = C.POINTER(C.c_int)
             lp = C.POINTER(C.c_int64)
-            r = self.lib.oracle_set_tfsf(self.h, self.incident.h, n, tc.ctypes.data_as(ip),
+            r = self.lib.oracle_set_tfsf(h, incident_handle, n, tc.ctypes.data_as(ip),
                                          nf.ctypes.data_as(ip), to.ctypes.data_as(lp),
                                          _dp(coef), _dp(r0), _dp(r1), smp.ctypes.data_as(lp))
             if r != 0:
                 raise ValueError("bad TFSF table")
-        self.n = 0.0
+        return h
 
     def __del__(self):
-        if getattr(self, "h", None):
-            self.lib.oracle_destroy(self.h)
-            self.h = None
+        for name in ("h", "h_im"):
+            if getattr(self, name, None):
+                self.lib.oracle_destroy(getattr(self, name))
+                setattr(self, name, None)
 
     def step(self, nsteps, src_values=None):
         from gmes_gb300.scene import source_values
         if src_values is None:
             src_values = source_values(self.scene, self.scene.dt, self.n, nsteps)
-        v = np.ascontiguousarray(src_values, np.float64)
-        if v.size == 0:
-            v = np.zeros(1)
+
+        def arr(a):
+            a = np.ascontiguousarray(a, np.float64)
+            return a if a.size else np.zeros(1)
+
+        aux = None
         if self.incident is not None:
-            a = np.ascontiguousarray(
-                source_values(self.incident.scene, self.scene.dt, self.n, nsteps), np.float64)
-            if a.size == 0:
-                a = np.zeros(1)
+            aux = source_values(self.incident.scene, self.scene.dt, self.n, nsteps)
+        if self.cmplx:
+            sv = np.asarray(src_values, np.complex128)
+            vr, vi = arr(sv.real), arr(sv.imag)
+            if aux is not None:
+                av = np.asarray(aux, np.complex128)
+                ar, ai = arr(av.real), arr(av.imag)
+                r = self.lib.oracle_step_complex(self.h, int(nsteps), _dp(vr), _dp(vi), _dp(ar),
+                                                 _dp(ai))
+            else:
+                r = self.lib.oracle_step_complex(self.h, int(nsteps), _dp(vr), _dp(vi), None,
+                                                 None)
+            if r != 0:
+                raise RuntimeError("complex oracle step failed")
+            if self.incident is not None:
+                self.incident.n += nsteps
+        elif self.incident is not None:
+            v, a = arr(src_values), arr(aux)
             self.lib.oracle_step_tfsf(self.h, int(nsteps), _dp(v), _dp(a))
             self.incident.n += nsteps
         else:
+            v = arr(src_values)
             self.lib.oracle_step(self.h, int(nsteps), _dp(v))
         self.n += nsteps
 
     def field(self, c):
         sh = self.scene.shape(c)
-        ptr = self.lib.oracle_field(self.h, c)
-        return np.ctypeslib.as_array(ptr, shape=sh).copy()
+        re = np.ctypeslib.as_array(self.lib.oracle_field(self.h, c), shape=sh).copy()
+        if not self.cmplx:
+            return re
+        im = np.ctypeslib.as_array(self.lib.oracle_field(self.h_im, c), shape=sh)
+        return re + 1j * im
 
     def fields(self):
         return [self.field(c) for c in range(6)]
@@ -195,6 +236,8 @@ class Oracle:
     def reset(self):
         """Zero the fields and every per-point state; time returns to 0."""
         self.lib.oracle_reset(self.h)
+        if self.h_im:
+            self.lib.oracle_reset(self.h_im)
         self.n = 0.0
         if self.incident is not None:
             self.incident.n = 0.0

@@ -28,14 +28,21 @@ def load_golden(name):
 
 
 def checksum(a):
+    a = np.asarray(a)
+    if np.iscomplexobj(a):
+        return [complex(np.sum(a)).real, complex(np.sum(a)).imag,
+                float(np.sum(np.abs(a) ** 2)), float(np.max(np.abs(a)))]
     a = np.asarray(a, np.float64)
     return [float(np.sum(a)), float(np.sum(a * a)), float(np.max(np.abs(a)))]
 
 
 def rel_l2(a, b):
     """Relative L2 error of a against reference b (0 when both are zero)."""
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if not (np.iscomplexobj(a) or np.iscomplexobj(b)):
+        a = a.astype(np.float64)
+        b = b.astype(np.float64)
     nb = np.linalg.norm(b)
     d = np.linalg.norm(a - b)
     return d / nb if nb > 0 else d

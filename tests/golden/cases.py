@@ -168,6 +168,45 @@ def tfsf3d(g, steps=60):
     return g.FDTD(space, geometry, sources, verbose=False), steps
 
 
+def bloch2d(g, steps=120):
+    """TMz with a Bloch boundary (complex fields, phase-shifted ghost copies),
+    no PML: a dielectric cylinder and a complex Continuous Ez source."""
+    space = g.Cartesian(size=(3, 3, 0), resolution=10)
+    geometry = [g.DefaultMedium(material=g.Dielectric()),
+                g.Sphere(material=g.Dielectric(eps_inf=3.0), center=(0.3, -0.2, 0), radius=0.6)]
+    sources = [g.PointSource(src_time=g.Continuous(freq=0.9, width=1.0), center=(-0.4, 0.1, 0),
+                             component=g.Ez)]
+    return g.TMzFDTD(space, geometry, sources, bloch=(0.5, 0.3, 0.0), verbose=False), steps
+
+
+def bloch3d(g, steps=60):
+    """3-D complex fields with a Bloch vector, a Drude sphere, a dielectric
+    block, CPML on all faces and a Bandpass Ex source."""
+    space = g.Cartesian(size=(1.6, 1.6, 1.6), resolution=10)
+    geometry = [g.DefaultMedium(material=g.Dielectric()),
+                g.Sphere(material=g.Drude(eps_inf=1, dps=(g.DrudePole(omega=3.0, gamma=0.3),)),
+                         center=(0.2, 0.1, 0), radius=0.3),
+                g.Block(material=g.Dielectric(eps_inf=2.5), center=(-0.3, 0, 0.2),
+                        size=(0.3, 0.8, 0.3)),
+                g.Shell(material=g.Cpml(), thickness=0.3)]
+    sources = [g.PointSource(src_time=g.Bandpass(freq=1.0, fwidth=1.0, s=3), center=(0, 0, 0),
+                             component=g.Ex)]
+    return g.FDTD(space, geometry, sources, bloch=(0.4, 0.2, 0.1), verbose=False), steps
+
+
+def bloch_tfsf2d(g, steps=100):
+    """Complex TMz with a TFSF plane wave (the incident-field grid is complex
+    too) and a Bloch vector along y."""
+    space = g.Cartesian(size=(4, 4, 0), resolution=10)
+    geometry = [g.DefaultMedium(material=g.Dielectric()),
+                g.Sphere(material=g.Dielectric(eps_inf=4.0), center=(0.3, 0, 0), radius=0.5),
+                g.Shell(material=g.Cpml(), thickness=0.6)]
+    sources = [g.TotalFieldScatteredField(src_time=g.Bandpass(freq=1.0, fwidth=1.0, s=3),
+                                          center=(0, 0, 0), size=(2.0, 2.0, 0),
+                                          direction=(1, 0, 0), polarization=(0, 0, 1))]
+    return g.TMzFDTD(space, geometry, sources, bloch=(0.0, 0.4, 0.0), verbose=False), steps
+
+
 CASES = {
     "tmz_regression": tmz_regression,
     "air2d": air2d,
@@ -178,6 +217,9 @@ CASES = {
     "tmx_cpml_hard": tmx_cpml_hard,
     "tfsf2d": tfsf2d,
     "tfsf3d": tfsf3d,
+    "bloch2d": bloch2d,
+    "bloch3d": bloch3d,
+    "bloch_tfsf2d": bloch_tfsf2d,
 }
 
 # Cases whose golden file stores only Ez in full (and checksums of the rest)

@@ -27,6 +27,10 @@ from cases import CASES, COMP_NAMES, SUMMARY_ONLY  # noqa: E402
 
 
 def checksum(a):
+    a = np.asarray(a)
+    if np.iscomplexobj(a):
+        return [complex(np.sum(a)).real, complex(np.sum(a)).imag,
+                float(np.sum(np.abs(a) ** 2)), float(np.max(np.abs(a)))]
     a = np.asarray(a, np.float64)
     return [float(np.sum(a)), float(np.sum(a * a)), float(np.max(np.abs(a)))]
 

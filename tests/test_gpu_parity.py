@@ -62,9 +62,17 @@ def test_strict_is_bit_exact_with_reference(name):
         assert np.array_equal(f, ref[c]), (name, cn, rel_l2(f, ref[c]))
 
 
+COMPLEX_CASES = {n for n in CASES if n.startswith("bloch")}
+
+
 @pytest.mark.parametrize("precision", ["fp64", "df64", "fp32"])
 @pytest.mark.parametrize("name", list(CASES))
 def test_fast_modes_within_tolerance(name, precision):
+    if name in COMPLEX_CASES and precision != "fp64":
+        # complex (Bloch) grids run in fp64 / fp64_strict only
+        with pytest.raises(ValueError):
+            run_case(name, precision)
+        return
     sim, _ = run_case(name, precision)
     ref = oracle_fields(name)
     for c, cn in enumerate(COMP_NAMES):

@@ -71,7 +71,8 @@ def test_updater_point_counts_match_reference():
         for comp in scene.active:
             want = {}
             for tname, count in meta["updaters"][comp.__name__].items():
-                kind = tname[:-len(comp.__name__) - len("Real")]
+                suffix = "Cmplx" if tname.endswith("Cmplx") else "Real"
+                kind = tname[:-len(comp.__name__) - len(suffix)]
                 want[kind] = want.get(kind, 0) + count
             got = {}
             for cid, count in scene.counts(comp.index).items():
