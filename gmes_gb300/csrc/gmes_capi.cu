@@ -307,7 +307,7 @@ gmes_status gmes_build_coefficients(const gmes_grid_desc* g, const gmes_class_de
   for (int c = 0; c < 6; ++c) {
     for (int i = 0; i < g->nclass[c]; ++i, ++k) {
       const gmes_class_desc& cd = classes[k];
-      if (cd.kind < GMES_KIND_DUMMY || cd.kind > GMES_KIND_CONST)
+      if (cd.kind < GMES_KIND_DUMMY || cd.kind > GMES_KIND_DCP_PLRC)
         return fail(GMES_ERR_VALUE, "component %d class %d: unknown kind %d", c, i, cd.kind);
       if ((cd.kind == GMES_KIND_CPML || cd.kind == GMES_KIND_UPML) &&
           (cd.pml < 0 || cd.pml >= g->npml))
@@ -330,12 +330,14 @@ gmes_status gmes_build_coefficients(const gmes_grid_desc* g, const gmes_class_de
         case GMES_KIND_LORENTZ: need = 2 + 3 * cd.npole; naux = 2 * cd.npole; break;
         case GMES_KIND_DCP: need = 2 + 2 * cd.npole + 5 * cd.ncp;
           naux = 1 + 2 * cd.npole + 2 * cd.ncp; break;
+        case GMES_KIND_DCP_PLRC: need = 3 + 5 * cd.npole + 9 * cd.ncp;
+          naux = cd.npole + 2 * cd.ncp; break;
         case GMES_KIND_CPML: naux = 2; break;
         case GMES_KIND_UPML: naux = 1; break;
         default: break;
       }
       const bool dispk = cd.kind == GMES_KIND_DRUDE || cd.kind == GMES_KIND_LORENTZ ||
-                         cd.kind == GMES_KIND_DCP;
+                         cd.kind == GMES_KIND_DCP || cd.kind == GMES_KIND_DCP_PLRC;
       if (dispk && c >= 3)
         return fail(GMES_ERR_VALUE, "component %d class %d: dispersive kinds are E-only", c, i);
       disp = disp || dispk;

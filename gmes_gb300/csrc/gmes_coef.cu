@@ -8,6 +8,7 @@
 //   Drude a, c                      src/material.pyx:1546-1565
 //   Lorentz a, c                    src/material.pyx:1727-1746
 //   DCP-ADE a, b, c                 src/material.pyx:1074-1105
+//   DCP-PLRC / RC a, b, c           src/material.pyx:1279-1370, 1474-1490
 //   PML sigma/kappa grading         src/material.pyx:442-502
 //   UPML c1..c6                     src/material.pyx:558-591
 //   CPML a, b, c                    src/material.pyx:795-820
@@ -28,6 +29,114 @@ __device__ double pml_depth(const gmes_pml_desc& p, double w, int axis) {
   if (w <= p.d - h) return fmin(fmax((h + w) / p.d, 0.0), 1.0);
   if (h - p.d <= w) return fmin(fmax((h - w) / p.d, 0.0), 1.0);
   return -1.0;
+}
+
+// Complex arithmetic of the reference's coefficient code (Python complex
+// numbers, src/material.pyx:1227-1490): product (ar br - ai bi,
+// ar bi + ai br) and Smith's quotient, the algorithm CPython's complex
+// division uses.  This file is compiled without FMA contraction.
+struct cplx {
+  double r, i;
+};
+__device__ inline cplx cmul(cplx a, cplx b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
+__device__ inline cplx cadd(cplx a, cplx b) { return {a.r + b.r, a.i + b.i}; }
+__device__ inline cplx csub(cplx a, cplx b) { return {a.r - b.r, a.i - b.i}; }
+__device__ inline cplx cdiv(cplx a, cplx b) {
+  const double abr = b.r < 0 ? -b.r : b.r, abi = b.i < 0 ? -b.i : b.i;
+  if (abr >= abi) {
+    if (abr == 0.0) return {0.0, 0.0};
+    const double ratio = b.i / b.r;
+    const double den = b.r + b.i * ratio;
+    return {(a.r + a.i * ratio) / den, (a.i - a.r * ratio) / den};
+  }
+  const double ratio = b.r / b.i;
+  const double den = b.r * ratio + b.i;
+  return {(a.r * ratio + a.i) / den, (a.i * ratio - a.r) / den};
+}
+
+// Python's sum() over floats (CPython 3.12 builtin sum): Neumaier
+// compensated summation, the compensation added when the float run ends.
+struct FloatSum {
+  double f = 0.0, c = 0.0;
+  int n = 0;
+  __device__ void add(double x) {
+    if (n++ == 0) {
+      f = x;
+      return;
+    }
+    const double t = f + x;
+    if (fabs(f) >= fabs(x))
+      c += (f - t) + x;
+    else
+      c += (x - t) + f;
+    f = t;
+  }
+  __device__ double value() const { return (c != 0.0 && isfinite(c)) ? f + c : f; }
+};
+
+// PLRC / RC coefficients of one DCP class (src/material.pyx:1279-1370):
+// a[p] = (dchi - dxi, dxi, exp(-gamma dt)) per Drude term,
+// b[q] = (dchi - dxi, dxi, exp(-dt (gamma + i omega))) per critical point,
+// c = (dt, eps - xi0 - cond, 1) / (eps - xi0 + chi0 + cond), where chi0 and
+// xi0 are sum() over the Drude terms (floats) then the critical points
+// (complex), real part.
+__device__ void plrc_coefficients(const double* p, int npole, int ncp, double dt, Coef* pool) {
+  const double eps_inf = p[0], sigma = p[1];
+  const bool rc = p[2] != 0.0;
+  const double* dp = p + 3;
+  const double* cp = dp + 5 * npole;
+  FloatSum chi_f, xi_f;
+  for (int q = 0; q < npole; ++q) {
+    const double omega = dp[5 * q], gamma = dp[5 * q + 1];
+    const double e_m = dp[5 * q + 2], e_p = dp[5 * q + 3], th = dp[5 * q + 4];
+    const double gdt = gamma * dt;
+    const double w = omega / gamma;
+    const double w2 = w * w;
+    const double chi = w2 * ((e_m + gdt) - 1.0);
+    const double k = 1.0 / (1.0 - e_p) + 1.0 / gdt;
+    const double xi = chi * k + w2 * (gdt / 2.0 / th - 1.0);
+    const double x = w * (1.0 - e_m);
+    const double dchi = -(x * x);
+    const double dxi = rc ? 0.0 : dchi * k;
+    pool[kPoolA + 3 * q + 0] = make_coef(dchi - dxi);
+    pool[kPoolA + 3 * q + 1] = make_coef(dxi);
+    pool[kPoolA + 3 * q + 2] = make_coef(e_m);
+    chi_f.add(chi);
+    if (!rc) xi_f.add(xi);
+  }
+  double chi0 = chi_f.value(), xi0 = rc ? 0.0 : xi_f.value();
+  for (int q = 0; q < ncp; ++q) {
+    const double* c = cp + 9 * q;
+    const double amp = c[0], omega = c[1], gamma = c[2];
+    const cplx P = {c[3], c[4]}, Q = {c[5], c[6]}, R = {c[7], c[8]};
+    const cplx go = {gamma, omega};
+    const cplx dtgo = cmul({dt, 0.0}, go);
+    const cplx one = {1.0, 0.0};
+    const cplx omq = csub(one, Q);
+    // 2j * amp * omega * exp(1j phi), left to right
+    const cplx pre = cmul(cmul(cmul({0.0, 2.0}, {amp, 0.0}), {omega, 0.0}), P);
+    const cplx chi = cdiv(cmul(pre, omq), go);
+    // (1 - Q)**2 as CPython's integer power: 1 * ((1 - Q) * (1 - Q))
+    const cplx dchi = cdiv(cmul(pre, cmul(one, cmul(omq, omq))), go);
+    const cplx k = cadd(cdiv(one, csub(one, R)), cdiv(one, dtgo));
+    const cplx xi = rc ? cplx{0.0, 0.0} : cmul(chi, k);
+    const cplx dxi = rc ? cplx{0.0, 0.0} : cmul(dchi, k);
+    const cplx b0 = csub(dchi, dxi);
+    pool[kPoolB + 6 * q + 0] = make_coef(b0.r);
+    pool[kPoolB + 6 * q + 1] = make_coef(b0.i);
+    pool[kPoolB + 6 * q + 2] = make_coef(dxi.r);
+    pool[kPoolB + 6 * q + 3] = make_coef(dxi.i);
+    pool[kPoolB + 6 * q + 4] = make_coef(Q.r);
+    pool[kPoolB + 6 * q + 5] = make_coef(Q.i);
+    chi0 = chi0 + chi.r;
+    xi0 = xi0 + xi.r;
+  }
+  const double cond = 0.5 * dt * sigma;
+  const double denom = ((eps_inf - xi0) + chi0) + cond;
+  pool[kPoolC + 0] = make_coef(dt / denom);
+  pool[kPoolC + 1] = make_coef(((eps_inf - xi0) - cond) / denom);
+  pool[kPoolC + 2] = make_coef(1.0 / denom);
+  pool[kPoolC + 3] = make_coef(0.0);
 }
 
 __global__ void k_build_classes(gmes_grid_desc g, CoefLayout L) {
@@ -92,6 +201,8 @@ __global__ void k_build_classes(gmes_grid_desc g, CoefLayout L) {
     pool[kPoolC + 1] = make_coef(-2.0 / denom);
     pool[kPoolC + 2] = make_coef((2.0 * eps_inf - dt * sigma) / denom);
     pool[kPoolC + 3] = make_coef(0.0);
+  } else if (cd.kind == GMES_KIND_DCP_PLRC) {
+    plrc_coefficients(p, cd.npole, cd.ncp, dt, pool);
   } else if (cd.kind == GMES_KIND_DCP) {
     const double eps_inf = p[0], sigma = p[1];
     double sum_a2 = 0.0, sum_b2 = 0.0, sum_b3 = 0.0, sum_b4 = 0.0;

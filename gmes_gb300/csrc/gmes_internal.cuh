@@ -49,10 +49,11 @@ struct ClassCoef {
 };
 
 // Dispersive coefficients of one class: a[p][3] (Drude/Lorentz poles or DCP
-// Drude terms), b[q][5] (DCP critical points), c[4].
+// Drude terms), b[q][5] (DCP-ADE critical points; DCP-PLRC: b0, b1, b2 as
+// re/im pairs, 6 per point), c[4].
 constexpr int kPoolA = 0;
 constexpr int kPoolB = 3 * GMES_MAX_POLES;
-constexpr int kPoolC = kPoolB + 5 * GMES_MAX_POLES;
+constexpr int kPoolC = kPoolB + 6 * GMES_MAX_POLES;
 constexpr int kPoolStride = kPoolC + 4;
 
 // PML profile entry at one index along one axis (5 coefficients):

@@ -200,6 +200,33 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
       P::st(fp, e_new);
       return;
     }
+    if (kind == GMES_KIND_DCP_PLRC) {
+      // src/pw_dcp.hh:466-583: psi_dp[npole] real, psi_cp[ncp] complex (re, im)
+      const int cb = cc.npole;
+      R psum = P::zero(), csum = P::zero();
+      for (int q = 0; q < cc.npole; ++q) psum = psum + P::ldw(aux + (int64_t)q * np + lin);
+      for (int q = 0; q < cc.ncp; ++q)
+        csum = csum + P::ldw(aux + (int64_t)(cb + 2 * q) * np + lin);
+      const R e_new = (P::cfg(&(pool[kPoolC])) * curl + P::cfg(&(pool[kPoolC + 1])) * e_now) +
+                      P::cfg(&(pool[kPoolC + 2])) * (psum + csum);
+      for (int q = 0; q < cc.npole; ++q) {
+        T* sp = aux + (int64_t)q * np + lin;
+        const Coef* a = pool + kPoolA + 3 * q;
+        P::st(sp, (P::cfg(a) * e_new + P::cfg(a + 1) * e_now) + P::cfg(a + 2) * P::ldw(sp));
+      }
+      for (int q = 0; q < cc.ncp; ++q) {
+        T* pr_ = aux + (int64_t)(cb + 2 * q) * np + lin;
+        T* pi_ = aux + (int64_t)(cb + 2 * q + 1) * np + lin;
+        const R pr = P::ldw(pr_), pi = P::ldw(pi_);
+        const Coef* b = pool + kPoolB + 6 * q;
+        P::st(pr_, (P::cfg(b) * e_new + P::cfg(b + 2) * e_now) +
+                       (P::cfg(b + 4) * pr - P::cfg(b + 5) * pi));
+        P::st(pi_, (P::cfg(b + 1) * e_new + P::cfg(b + 3) * e_now) +
+                       (P::cfg(b + 4) * pi + P::cfg(b + 5) * pr));
+      }
+      P::st(fp, e_new);
+      return;
+    }
   }
 }
 
@@ -330,6 +357,33 @@ __device__ __forceinline__ void update_strict(const GridDev& g, int64_t lin, con
         *pnp = p_new;
       }
       *eo = e_now;
+      *fp = e_new;
+      return;
+    }
+    if (kind == GMES_KIND_DCP_PLRC) {
+      // src/pw_dcp.hh:466-583 in its operation order; psi_cp complex
+      // products as (ac - bd, ad + bc)
+      const int cb = cc.npole;
+      double psum = 0.0, csum = 0.0;
+      for (int q = 0; q < cc.npole; ++q) psum = ADD(psum, aux[(int64_t)q * np + lin]);
+      for (int q = 0; q < cc.ncp; ++q) csum = ADD(csum, aux[(int64_t)(cb + 2 * q) * np + lin]);
+      const double e_new = ADD(ADD(MUL(pool[kPoolC].d, curl), MUL(pool[kPoolC + 1].d, e_now)),
+                               MUL(pool[kPoolC + 2].d, ADD(psum, csum)));
+      for (int q = 0; q < cc.npole; ++q) {
+        double* sp = aux + (int64_t)q * np + lin;
+        const Coef* a = pool + kPoolA + 3 * q;
+        *sp = ADD(ADD(MUL(a[0].d, e_new), MUL(a[1].d, e_now)), MUL(a[2].d, *sp));
+      }
+      for (int q = 0; q < cc.ncp; ++q) {
+        double* pr_ = aux + (int64_t)(cb + 2 * q) * np + lin;
+        double* pi_ = aux + (int64_t)(cb + 2 * q + 1) * np + lin;
+        const double pr = *pr_, pi = *pi_;
+        const Coef* b = pool + kPoolB + 6 * q;
+        *pr_ = ADD(ADD(MUL(b[0].d, e_new), MUL(b[2].d, e_now)),
+                   SUB(MUL(b[4].d, pr), MUL(b[5].d, pi)));
+        *pi_ = ADD(ADD(MUL(b[1].d, e_new), MUL(b[3].d, e_now)),
+                   ADD(MUL(b[4].d, pi), MUL(b[5].d, pr)));
+      }
       *fp = e_new;
       return;
     }

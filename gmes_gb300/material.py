@@ -14,7 +14,8 @@ The host-side ``init()`` coefficients (``a``, ``b``, ``c``, ``sigma_max``)
 are kept because user code and the CPU oracle read them.
 """
 
-from math import cos, exp, sin, sqrt
+from cmath import exp as cexp
+from math import cos, exp, sin, sqrt, tanh
 
 import numpy as np
 
@@ -29,11 +30,12 @@ KIND_DRUDE = 4
 KIND_LORENTZ = 5
 KIND_DCP = 6
 KIND_CONST = 7
+KIND_DCP_PLRC = 8
 
 KIND_NAMES = {
     KIND_DUMMY: "Dummy", KIND_DIELECTRIC: "Dielectric", KIND_CPML: "Cpml",
     KIND_UPML: "Upml", KIND_DRUDE: "Drude", KIND_LORENTZ: "Lorentz",
-    KIND_DCP: "DcpAde", KIND_CONST: "Const",
+    KIND_DCP: "DcpAde", KIND_CONST: "Const", KIND_DCP_PLRC: "DcpPlrc",
 }
 
 
@@ -399,12 +401,118 @@ class _Unsupported(Dielectric):
         raise NotImplementedError(f"{type(self).__name__}: {self.reason}")
 
 
-class DcpPlrc(_Unsupported):
-    reason = "the PLRC form of the DCP model is not implemented; use DcpAde"
+class DcpPlrc(Dielectric):
+    """Drude-critical-points medium, piecewise-linear recursive convolution
+    (src/material.pyx:1227-1471, src/pw_dcp.hh:406-746).
+
+    ``init()`` keeps the reference's host coefficients a, b, c; the engine
+    recomputes them in FP64 on the GPU from the physical parameters and the
+    transcendental values taken here with the host libm.
+    """
+
+    rc = False
+
+    def __init__(self, eps_inf=1, mu_inf=1, sigma=0, dps=(), cps=()):
+        super().__init__(eps_inf, mu_inf)
+        self.sigma = float(sigma)
+        self.dps = tuple(dps)
+        self.cps = tuple(cps)
+        self.initialized = False
+
+    def init(self, space, param=None):
+        self.dt = space.dt
+        self.a = np.empty((len(self.dps), 3), np.double)
+        for i, pole in enumerate(self.dps):
+            self.a[i, 0] = self.delta_chi_dp_0(pole) - self.delta_xi_dp_0(pole)
+            self.a[i, 1] = self.delta_xi_dp_0(pole)
+            self.a[i, 2] = exp(-pole.gamma * self.dt)
+        self.b = np.empty((len(self.cps), 3), complex)
+        for i, pnt in enumerate(self.cps):
+            self.b[i, 0] = self.delta_chi_cp_0(pnt) - self.delta_xi_cp_0(pnt)
+            self.b[i, 1] = self.delta_xi_cp_0(pnt)
+            self.b[i, 2] = cexp(-self.dt * (pnt.gamma + 1j * pnt.omega))
+        chi_0 = (sum([self.chi_dp_0(p) for p in self.dps] +
+                     [self.chi_cp_0(p) for p in self.cps]) + 0j).real
+        xi_0 = (sum([self.xi_dp_0(p) for p in self.dps] +
+                    [self.xi_cp_0(p) for p in self.cps]) + 0j).real
+        self.c = np.empty(3, np.double)
+        conductivity = 0.5 * self.dt * self.sigma
+        denom = self.eps_inf - xi_0 + chi_0 + conductivity
+        self.c[0] = self.dt / denom
+        self.c[1] = (self.eps_inf - xi_0 - conductivity) / denom
+        self.c[2] = 1 / denom
+        self.initialized = True
+
+    # the susceptibility terms of src/material.pyx:1313-1356
+    def chi_dp_0(self, dp):
+        gdt = dp.gamma * self.dt
+        return (dp.omega / dp.gamma) ** 2 * (exp(-gdt) + gdt - 1)
+
+    def xi_dp_0(self, dp):
+        gdt = dp.gamma * self.dt
+        return (self.chi_dp_0(dp) * (1 / (1 - exp(gdt)) + 1 / gdt)
+                + (dp.omega / dp.gamma) ** 2 * (gdt / 2 / tanh(gdt / 2) - 1))
+
+    def delta_chi_dp_0(self, dp):
+        gdt = dp.gamma * self.dt
+        return -(dp.omega / dp.gamma * (1 - exp(-gdt))) ** 2
+
+    def delta_xi_dp_0(self, dp):
+        gdt = dp.gamma * self.dt
+        return self.delta_chi_dp_0(dp) * (1 / (1 - exp(gdt)) + 1 / gdt)
+
+    def chi_cp_0(self, cp):
+        go = cp.gamma + 1j * cp.omega
+        return 2j * cp.amp * cp.omega * cexp(1j * cp.phi) * (1 - cexp(-self.dt * go)) / go
+
+    def xi_cp_0(self, cp):
+        dtgo = self.dt * (cp.gamma + 1j * cp.omega)
+        return self.chi_cp_0(cp) * (1 / (1 - cexp(dtgo)) + 1 / dtgo)
+
+    def delta_chi_cp_0(self, cp):
+        go = cp.gamma + 1j * cp.omega
+        return 2j * cp.amp * cp.omega * cexp(1j * cp.phi) * (1 - cexp(-self.dt * go)) ** 2 / go
+
+    def delta_xi_cp_0(self, cp):
+        dtgo = self.dt * (cp.gamma + 1j * cp.omega)
+        return self.delta_chi_cp_0(cp) * (1 / (1 - cexp(dtgo)) + 1 / dtgo)
+
+    def engine_class(self, comp, underneath=None):
+        if comp.index >= 3:
+            return ClassDesc(KIND_DIELECTRIC, self._own(comp, underneath))
+        dt = self.dt
+        params = [self.eps_inf, self.sigma, 1.0 if self.rc else 0.0]
+        for p in self.dps:
+            gdt = p.gamma * dt
+            params += [p.omega, p.gamma, exp(-gdt), exp(gdt), tanh(gdt / 2)]
+        for p in self.cps:
+            go = p.gamma + 1j * p.omega
+            ph = cexp(1j * p.phi)
+            q = cexp(-dt * go)
+            r = cexp(dt * go)
+            params += [p.amp, p.omega, p.gamma, ph.real, ph.imag, q.real, q.imag,
+                       r.real, r.imag]
+        return ClassDesc(KIND_DCP_PLRC, self._own(comp, underneath), params,
+                         ndrude=len(self.dps), ncp=len(self.cps))
 
 
-class DcpRc(_Unsupported):
-    reason = "the RC form of the DCP model is not implemented; use DcpAde"
+class DcpRc(DcpPlrc):
+    """Drude-critical-points medium, recursive convolution (src/material.pyx:1474-1490):
+    the PLRC updater with the xi terms set to zero."""
+
+    rc = True
+
+    def xi_dp_0(self, dp):
+        return 0
+
+    def xi_cp_0(self, cp):
+        return 0j
+
+    def delta_xi_dp_0(self, dp):
+        return 0
+
+    def delta_xi_cp_0(self, cp):
+        return 0j
 
 
 class Dm2(_Unsupported):

@@ -16,8 +16,8 @@ import numpy as np
 
 from . import constant as const
 from .geometry import rasterize
-from .material import (KIND_CPML, KIND_DCP, KIND_DRUDE, KIND_DUMMY, KIND_LORENTZ,
-                       KIND_UPML, ClassDesc, Cpml)
+from .material import (KIND_CPML, KIND_DCP, KIND_DCP_PLRC, KIND_DRUDE, KIND_DUMMY,
+                       KIND_LORENTZ, KIND_UPML, ClassDesc, Cpml)
 
 MAX_CLASSES = 256
 
@@ -32,6 +32,8 @@ def naux_of(desc):
         return 2 * desc.ndrude
     if desc.kind == KIND_DCP:
         return 1 + 2 * desc.ndrude + 2 * desc.ncp
+    if desc.kind == KIND_DCP_PLRC:
+        return desc.ndrude + 2 * desc.ncp
     return 0
 
 
@@ -87,7 +89,7 @@ class Scene:
 
     @property
     def dispersive(self):
-        return any(d.kind in (KIND_DRUDE, KIND_LORENTZ, KIND_DCP)
+        return any(d.kind in (KIND_DRUDE, KIND_LORENTZ, KIND_DCP, KIND_DCP_PLRC)
                    for c in range(3) for d in self.classes[c])
 
     @property

@@ -75,7 +75,8 @@ typedef enum {
   GMES_KIND_DRUDE = 4,      /* src/pw_drude.hh (E side; H side is DIELECTRIC) */
   GMES_KIND_LORENTZ = 5,    /* src/pw_lorentz.hh */
   GMES_KIND_DCP = 6,        /* src/pw_dcp.hh, DcpAde* (ADE form) */
-  GMES_KIND_CONST = 7       /* src/pw_const.hh */
+  GMES_KIND_CONST = 7,      /* src/pw_const.hh */
+  GMES_KIND_DCP_PLRC = 8    /* src/pw_dcp.hh:406-746, DcpPlrc* (PLRC / RC forms) */
 } gmes_kind;
 
 /* gmes_grid_desc.flags */
@@ -104,6 +105,13 @@ enum { GMES_EX = 0, GMES_EY = 1, GMES_EZ = 2, GMES_HX = 3, GMES_HY = 4, GMES_HZ 
  *            (amp, cos phi, sin phi, omega, gamma) per critical point
  *            (src/material.pyx:1074-1105; the phase enters only through
  *            cos/sin, supplied by the caller's libm)
+ *   DCP_PLRC: eps_inf, sigma, rc (1: the RC form, DcpRc), then per Drude
+ *            term (omega, gamma, exp(-gamma dt), exp(gamma dt),
+ *            tanh(gamma dt / 2)), per critical point (amp, omega, gamma,
+ *            cos phi, sin phi, re/im of exp(-dt (gamma + i omega)), re/im of
+ *            exp(dt (gamma + i omega))) (src/material.pyx:1227-1490; the
+ *            caller's libm supplies every transcendental value, the GPU does
+ *            the complex arithmetic)
  */
 typedef struct {
   int32_t kind;      /* gmes_kind */

@@ -35,7 +35,7 @@
 #endif
 
 enum { K_DUMMY = 0, K_DIEL = 1, K_CPML = 2, K_UPML = 3, K_DRUDE = 4, K_LORENTZ = 5,
-       K_DCP = 6, K_CONST = 7 };
+       K_DCP = 6, K_CONST = 7, K_DCP_PLRC = 8 };
 #define MAXP 8
 #define MAXCLS 256
 #define MAXPML 4
@@ -43,11 +43,12 @@ enum { K_DUMMY = 0, K_DIEL = 1, K_CPML = 2, K_UPML = 3, K_DRUDE = 4, K_LORENTZ =
 typedef struct {
   int kind, pml, npole, ncp;
   double eps;
-  double params[2 + 2 * MAXP + 5 * MAXP];
+  double params[3 + 5 * MAXP + 9 * MAXP];
   int nparams;
   /* dispersive coefficients (per class, copied into every point by the reference) */
   double a[MAXP][3];
   double b[MAXP][5];
+  double bc[MAXP][6]; /* DcpPlrc: b0, b1, b2 as (re, im) */
   double c[4];
 } oclass;
 
@@ -173,8 +174,100 @@ static double upml_c6(const opml* p, double dt, double w, int ax) {
   return 2 * pml_kappa(p, w, ax) - pml_sigma(p, w, ax) * dt;
 }
 
+/* ---- Python complex arithmetic (src/material.pyx computes the DcpPlrc
+   coefficients with Python complex numbers): product (ac - bd, ad + bc)
+   and CPython's quotient (Smith's algorithm). */
+typedef struct { double r, i; } cpx;
+static cpx cmul(cpx a, cpx b) { cpx z = {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; return z; }
+static cpx cadd(cpx a, cpx b) { cpx z = {a.r + b.r, a.i + b.i}; return z; }
+static cpx csub(cpx a, cpx b) { cpx z = {a.r - b.r, a.i - b.i}; return z; }
+static cpx cdiv(cpx a, cpx b) {
+  const double abr = b.r < 0 ? -b.r : b.r, abi = b.i < 0 ? -b.i : b.i;
+  cpx z = {0, 0};
+  if (abr >= abi) {
+    if (abr == 0.0) return z;
+    const double ratio = b.i / b.r, den = b.r + b.i * ratio;
+    z.r = (a.r + a.i * ratio) / den;
+    z.i = (a.i - a.r * ratio) / den;
+  } else {
+    const double ratio = b.r / b.i, den = b.r * ratio + b.i;
+    z.r = (a.r * ratio + a.i) / den;
+    z.i = (a.i * ratio - a.r) / den;
+  }
+  return z;
+}
+
+/* Python's sum() over floats (CPython 3.12): Neumaier compensated
+   summation, the compensation added when the float run ends. */
+typedef struct { double f, c; int n; } fsum;
+static void fsum_add(fsum* s, double x) {
+  if (s->n++ == 0) { s->f = x; return; }
+  const double t = s->f + x;
+  if (fabs(s->f) >= fabs(x)) s->c += (s->f - t) + x; else s->c += (x - t) + s->f;
+  s->f = t;
+}
+static double fsum_value(const fsum* s) { return (s->c != 0 && isfinite(s->c)) ? s->f + s->c : s->f; }
+
+/* DcpPlrc / DcpRc coefficients (src/material.pyx:1279-1370, 1474-1490) from
+   eps_inf, sigma, rc, per Drude term (omega, gamma, exp(-g dt), exp(g dt),
+   tanh(g dt / 2)), per critical point (amp, omega, gamma, cos phi, sin phi,
+   exp(-dt (g + i w)), exp(dt (g + i w))). */
+static void init_plrc(oclass* k, double dt) {
+  const double* p = k->params;
+  const double eps_inf = p[0], sigma = p[1];
+  const int rc = p[2] != 0.0;
+  const double* dp = p + 3;
+  const double* cp = dp + 5 * k->npole;
+  fsum chi_f = {0, 0, 0}, xi_f = {0, 0, 0};
+  for (int q = 0; q < k->npole; ++q) {
+    const double omega = dp[5 * q], gamma = dp[5 * q + 1];
+    const double e_m = dp[5 * q + 2], e_p = dp[5 * q + 3], th = dp[5 * q + 4];
+    const double gdt = gamma * dt, w = omega / gamma, w2 = w * w;
+    const double chi = w2 * ((e_m + gdt) - 1.0);
+    const double kk = 1.0 / (1.0 - e_p) + 1.0 / gdt;
+    const double xi = chi * kk + w2 * (gdt / 2.0 / th - 1.0);
+    const double x = w * (1.0 - e_m);
+    const double dchi = -(x * x);
+    const double dxi = rc ? 0.0 : dchi * kk;
+    k->a[q][0] = dchi - dxi;
+    k->a[q][1] = dxi;
+    k->a[q][2] = e_m;
+    fsum_add(&chi_f, chi);
+    if (!rc) fsum_add(&xi_f, xi);
+  }
+  double chi0 = fsum_value(&chi_f), xi0 = rc ? 0.0 : fsum_value(&xi_f);
+  for (int q = 0; q < k->ncp; ++q) {
+    const double* c = cp + 9 * q;
+    const double amp = c[0], omega = c[1], gamma = c[2];
+    const cpx P = {c[3], c[4]}, Q = {c[5], c[6]}, R = {c[7], c[8]};
+    const cpx go = {gamma, omega}, one = {1.0, 0.0}, dtr = {dt, 0.0};
+    const cpx dtgo = cmul(dtr, go);
+    const cpx omq = csub(one, Q);
+    const cpx two_j = {0.0, 2.0}, ampc = {amp, 0.0}, omc = {omega, 0.0};
+    const cpx pre = cmul(cmul(cmul(two_j, ampc), omc), P);
+    const cpx chi = cdiv(cmul(pre, omq), go);
+    const cpx dchi = cdiv(cmul(pre, cmul(one, cmul(omq, omq))), go);
+    const cpx kk = cadd(cdiv(one, csub(one, R)), cdiv(one, dtgo));
+    const cpx zero = {0.0, 0.0};
+    const cpx xi = rc ? zero : cmul(chi, kk);
+    const cpx dxi = rc ? zero : cmul(dchi, kk);
+    const cpx b0 = csub(dchi, dxi);
+    k->bc[q][0] = b0.r; k->bc[q][1] = b0.i;
+    k->bc[q][2] = dxi.r; k->bc[q][3] = dxi.i;
+    k->bc[q][4] = Q.r; k->bc[q][5] = Q.i;
+    chi0 = chi0 + chi.r;
+    xi0 = xi0 + xi.r;
+  }
+  const double cond = 0.5 * dt * sigma;
+  const double denom = ((eps_inf - xi0) + chi0) + cond;
+  k->c[0] = dt / denom;
+  k->c[1] = ((eps_inf - xi0) - cond) / denom;
+  k->c[2] = 1 / denom;
+}
+
 /* ---- dispersive coefficients --------------------------------------------- */
 static void init_dispersive(oclass* k, double dt) {
+  if (k->kind == K_DCP_PLRC) { init_plrc(k, dt); return; }
   const double* p = k->params;
   if (k->kind == K_DRUDE || k->kind == K_LORENTZ) {
     double eps_inf = p[0], sigma = p[1];
@@ -307,7 +400,7 @@ int oracle_set_class_map(oracle* o, int c, const uint8_t* map) {
       case K_DIEL: sz = sizeof(p_diel); break;
       case K_CPML: sz = sizeof(p_cpml); break;
       case K_UPML: sz = sizeof(p_upml); break;
-      case K_DRUDE: case K_LORENTZ: case K_DCP: sz = sizeof(p_ade); break;
+      case K_DRUDE: case K_LORENTZ: case K_DCP: case K_DCP_PLRC: sz = sizeof(p_ade); break;
       default: sz = sizeof(p_plain); break;
     }
     u->pts = calloc((size_t)count[k], sz);
@@ -358,7 +451,7 @@ int oracle_set_class_map(oracle* o, int c, const uint8_t* map) {
         p->d = 0;
         break;
       }
-      case K_DRUDE: case K_LORENTZ: case K_DCP: {
+      case K_DRUDE: case K_LORENTZ: case K_DCP: case K_DCP_PLRC: {
         p_ade* p = (p_ade*)u->pts + u->count;
         p->off = t; memcpy(p->idx, idx, sizeof(idx));
         break;
@@ -552,6 +645,36 @@ static void run_updater(oracle* o, const updater* u) {
                      cl->b[i][3] * e_now + cl->b[i][4] * e_new;
         for (int i = 0; i < Q; ++i) { p_old[i] = p_now[i]; p_now[i] = p_new[i]; }
         *e_old = e_now;
+        f[p->off] = e_new;
+      }
+      break;
+    }
+    case K_DCP_PLRC: {
+      /* src/pw_dcp.hh:466-583: e_new from the curl, e_now and the total
+         accumulator, then psi_dp[P] (real) and psi_cp[Q] (complex) */
+      p_ade* pts = (p_ade*)u->pts;
+      const int P = cl->npole, Q = cl->ncp;
+#pragma omp parallel for schedule(static) if (count >= o->omp_threshold)
+      for (int64_t t = 0; t < count; ++t) {
+        p_ade* p = &pts[t];
+        double D1, D2;
+        diffs(o, c, p->idx, &D1, &D2);
+        double* psi_dp = p->st;
+        double* psi_cp = p->st + P; /* (re, im) pairs */
+        const double e_now = f[p->off];
+        double sdp = 0, scp = 0;
+        for (int i = 0; i < P; ++i) sdp += psi_dp[i];
+        for (int i = 0; i < Q; ++i) scp += psi_cp[2 * i];
+        const double e_new = cl->c[0] * (D1 / d1 - D2 / d2) + cl->c[1] * e_now +
+                             cl->c[2] * (sdp + scp);
+        for (int i = 0; i < P; ++i)
+          psi_dp[i] = cl->a[i][0] * e_new + cl->a[i][1] * e_now + cl->a[i][2] * psi_dp[i];
+        for (int i = 0; i < Q; ++i) {
+          const double pr = psi_cp[2 * i], pi = psi_cp[2 * i + 1];
+          const double* b = cl->bc[i];
+          psi_cp[2 * i] = b[0] * e_new + b[2] * e_now + (b[4] * pr - b[5] * pi);
+          psi_cp[2 * i + 1] = b[1] * e_new + b[3] * e_now + (b[4] * pi + b[5] * pr);
+        }
         f[p->off] = e_new;
       }
       break;
@@ -778,7 +901,8 @@ int oracle_reset(oracle* o) {
       for (int64_t t = 0; t < u->count; ++t) {
         if (u->kind == K_CPML) { ((p_cpml*)u->pts)[t].psi1 = 0; ((p_cpml*)u->pts)[t].psi2 = 0; }
         else if (u->kind == K_UPML) ((p_upml*)u->pts)[t].d = 0;
-        else if (u->kind == K_DRUDE || u->kind == K_LORENTZ || u->kind == K_DCP)
+        else if (u->kind == K_DRUDE || u->kind == K_LORENTZ || u->kind == K_DCP ||
+                 u->kind == K_DCP_PLRC)
           memset(((p_ade*)u->pts)[t].st, 0, sizeof(((p_ade*)u->pts)[t].st));
       }
     }

@@ -299,6 +299,39 @@ void bind_all(py::module_& m, const std::string& sfx) {
   def_magnetic<T, DcpAdeHx>(m, "DcpAdeHx" + sfx);
   def_magnetic<T, DcpAdeHy>(m, "DcpAdeHy" + sfx);
   def_magnetic<T, DcpAdeHz>(m, "DcpAdeHz" + sfx);
+
+  // Drude-critical points, PLRC form (DcpRc uses it with other coefficients)
+  py::class_<DcpPlrcElectricParam<T>, ElectricParam<T>>(
+      m, ("DcpPlrcElectricParam" + sfx).c_str())
+      .def(py::init<>())
+      .def("set", [](DcpPlrcElectricParam<T>& p, py::array_t<double, py::array::c_style> a,
+                     py::array_t<std::complex<double>, py::array::c_style> b,
+                     py::array_t<double, py::array::c_style> c) {
+        if (a.ndim() != 2 || a.shape(1) != 3 || b.ndim() != 2 || b.shape(1) != 3 ||
+            c.ndim() != 1 || c.shape(0) != 3)
+          throw py::value_error(
+              "DcpPlrc coefficients require shapes (n, 3), (n, 3), and (3,)");
+        for (auto& r : rows3(a, "bad a")) p.a.push_back(r);
+        for (py::ssize_t i = 0; i < b.shape(0); ++i) {
+          std::array<std::complex<double>, 3> r;
+          for (int j = 0; j < 3; ++j) r[j] = b.at(i, j);
+          p.b.push_back(r);
+        }
+        for (int i = 0; i < 3; ++i) p.c[i] = c.at(i);
+        p.psi_dp_re.resize(a.shape(0));
+        p.psi_dp_im.resize(a.shape(0));
+        p.psi_cp_re.resize(b.shape(0));
+        p.psi_cp_im.resize(b.shape(0));
+      });
+  py::class_<DcpPlrcMagneticParam<T>, MagneticParam<T>>(
+      m, ("DcpPlrcMagneticParam" + sfx).c_str())
+      .def(py::init<>());
+  def_electric<T, DcpPlrcEx>(m, "DcpPlrcEx" + sfx);
+  def_electric<T, DcpPlrcEy>(m, "DcpPlrcEy" + sfx);
+  def_electric<T, DcpPlrcEz>(m, "DcpPlrcEz" + sfx);
+  def_magnetic<T, DcpPlrcHx>(m, "DcpPlrcHx" + sfx);
+  def_magnetic<T, DcpPlrcHy>(m, "DcpPlrcHy" + sfx);
+  def_magnetic<T, DcpPlrcHz>(m, "DcpPlrcHz" + sfx);
 }
 
 }  // namespace

@@ -207,6 +207,42 @@ def bloch_tfsf2d(g, steps=100):
     return g.TMzFDTD(space, geometry, sources, bloch=(0.0, 0.4, 0.0), verbose=False), steps
 
 
+def dcp_plrc3d(g, steps=80, courant_ratio=0.6):
+    """DcpPlrc (PLRC form) and DcpRc (RC form) Drude-critical-points media
+    (src/pw_dcp.hh:406-746) in an eps = 2.25 background, CPML, Bandpass Ez."""
+    rng = np.random.default_rng(3)
+    cps = tuple(g.CriticalPoint(amp=float(rng.uniform(0.5, 2.0)),
+                                phi=float(rng.uniform(-1.5, 1.5)),
+                                omega=float(rng.uniform(2.0, 5.0)),
+                                gamma=float(rng.uniform(0.2, 1.0))) for _ in range(2))
+    space = g.Cartesian(size=(2.0, 2.0, 2.0), resolution=10)
+    geometry = [
+        g.DefaultMedium(material=g.Dielectric(eps_inf=2.25)),
+        g.Sphere(material=g.DcpPlrc(eps_inf=1.1, dps=(g.DrudePole(omega=7.0, gamma=0.2),),
+                                    cps=cps), center=(-0.25, 0.2, 0.1), radius=0.35),
+        g.Block(material=g.DcpRc(eps_inf=1.5, sigma=0.1,
+                                 dps=(g.DrudePole(omega=4.0, gamma=0.5),), cps=cps[:1]),
+                center=(0.3, -0.2, -0.1), size=(0.4, 0.5, 0.6)),
+        g.Shell(material=g.Cpml(), thickness=0.4),
+    ]
+    sources = [g.PointSource(src_time=g.Bandpass(freq=0.8, fwidth=1.0, s=3), center=(0, 0, 0),
+                             component=g.Ez)]
+    return g.FDTD(space, geometry, sources, verbose=False, courant_ratio=courant_ratio), steps
+
+
+def dcp_plrc_bloch2d(g, steps=100):
+    """Complex TMz with a Bloch vector and a DcpPlrc cylinder (the PLRC
+    accumulators of the real and imaginary parts are separate)."""
+    space = g.Cartesian(size=(3, 3, 0), resolution=10)
+    cps = (g.CriticalPoint(amp=1.2, phi=0.4, omega=3.0, gamma=0.5),)
+    geometry = [g.DefaultMedium(material=g.Dielectric()),
+                g.Sphere(material=g.DcpPlrc(eps_inf=1.5, dps=(g.DrudePole(omega=5.0, gamma=0.3),),
+                                            cps=cps), center=(0.2, -0.1, 0), radius=0.6)]
+    sources = [g.PointSource(src_time=g.Continuous(freq=0.7, width=1.0), center=(-0.5, 0.2, 0),
+                             component=g.Ez)]
+    return g.TMzFDTD(space, geometry, sources, bloch=(0.3, -0.2, 0.0), verbose=False), steps
+
+
 CASES = {
     "tmz_regression": tmz_regression,
     "air2d": air2d,
@@ -220,6 +256,8 @@ CASES = {
     "bloch2d": bloch2d,
     "bloch3d": bloch3d,
     "bloch_tfsf2d": bloch_tfsf2d,
+    "dcp_plrc3d": dcp_plrc3d,
+    "dcp_plrc_bloch2d": dcp_plrc_bloch2d,
 }
 
 # Cases whose golden file stores only Ez in full (and checksums of the rest)

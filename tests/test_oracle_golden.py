@@ -79,7 +79,7 @@ def test_updater_point_counts_match_reference():
                 k = KIND_NAMES[scene.classes[comp.index][cid].kind]
                 got[k] = got.get(k, 0) + count
             # the reference's Drude/Lorentz/DcpAde H updaters are plain dielectric here
-            for k in ("Drude", "Lorentz", "DcpAde"):
+            for k in ("Drude", "Lorentz", "DcpAde", "DcpPlrc"):
                 if comp.index >= 3 and k in want:
                     want["Dielectric"] = want.get("Dielectric", 0) + want.pop(k)
             assert got == want, (name, comp.__name__)
