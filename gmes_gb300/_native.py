@@ -29,7 +29,7 @@ EXPORTS = [
     "gmes_graph_capture_step", "gmes_graph_capture_batch", "gmes_graph_launch",
     "gmes_graph_destroy", "gmes_rasterize", "gmes_batch_step_noalloc",
     "gmes_tmz_sizes", "gmes_tmz_check", "gmes_tmz_set_design", "gmes_tmz_reset",
-    "gmes_tmz_forward", "gmes_tmz_objective", "gmes_tmz_adjoint",
+    "gmes_tmz_forward", "gmes_tmz_objective", "gmes_tmz_adjoint", "gmes_points_update",
 ]
 NOALLOC_MAX_GRIDS = 64
 
@@ -112,6 +112,14 @@ class TmzBatchC(C.Structure):
                 ("weight", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p)]
 
 
+class PointsC(C.Structure):
+    _fields_ = [("comp", C.c_int32), ("kind", C.c_int32), ("npoints", C.c_int32),
+                ("nparam", C.c_int32), ("nstate", C.c_int32), ("npole", C.c_int32),
+                ("ncp", C.c_int32), ("cmplx", C.c_int32), ("idx", C.c_void_p),
+                ("param", C.c_void_p), ("state", C.c_void_p),
+                ("shape", (C.c_int64 * 3) * 3)]
+
+
 class GmesError(RuntimeError):
     """Base of the errors raised for a failed engine call."""
 
@@ -172,6 +180,8 @@ def load():
     lib.gmes_tmz_forward.argtypes = [G, B, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]
     lib.gmes_tmz_objective.argtypes = [G, B, C.c_int32, C.c_void_p, C.c_void_p]
     lib.gmes_tmz_adjoint.argtypes = [G, B, C.c_int32, C.c_int32, C.c_void_p]
+    lib.gmes_points_update.argtypes = [P(PointsC), C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_double, C.c_double, C.c_double, C.c_void_p]
     for name in EXPORTS:
         if name not in ("gmes_abi_version", "gmes_last_error", "gmes_elem_size",
                         "gmes_batch_workspace_size"):

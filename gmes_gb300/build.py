@@ -25,7 +25,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 # Per-file flags: the coefficient builder and the rasteriser reproduce the
 # reference's FP64 operation order, so multiply-add contraction is disabled.
 EXTRA = {"gmes_coef.cu": ["--fmad=false"], "gmes_raster.cu": ["--fmad=false"]}
-SOURCES = ["gmes_capi.cu", "gmes_coef.cu", "gmes_step.cu", "gmes_raster.cu", "gmes_adjoint.cu"]
+SOURCES = ["gmes_capi.cu", "gmes_coef.cu", "gmes_step.cu", "gmes_raster.cu", "gmes_adjoint.cu",
+           "gmes_points.cu"]
 
 
 def nvcc():

@@ -222,6 +222,7 @@ int64_t max_ghost_plane(const GridDev& d) {
 // past its real plane.
 GridDev make_im_view(const GridDev& re, const gmes_grid_desc& g) {
   GridDev d = re;
+  d.part = 1;
   const int64_t es = elem_size(g.precision);
   for (int c = 0; c < 6; ++c) {
     d.f[c] = static_cast<char*>(re.f[c]) + re.npts[c] * es;
@@ -944,6 +945,47 @@ gmes_status gmes_tmz_adjoint(const gmes_grid_desc* g, const gmes_tmz_batch* b, i
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Point-list updaters (gmes_points.cu).
+// ---------------------------------------------------------------------------
+extern "C" gmes_status gmes_points_update(const gmes_points* p, void* inplace, const void* in1,
+                                          const void* in2, double d1, double d2, double dt,
+                                          void* stream) {
+  if (p == nullptr || inplace == nullptr || in1 == nullptr || in2 == nullptr)
+    return fail(GMES_ERR_VALUE, "NULL argument");
+  if (p->comp < 0 || p->comp > 5) return fail(GMES_ERR_INDEX, "component %d outside [0, 5]", p->comp);
+  if (p->kind < GMES_KIND_DUMMY || p->kind > GMES_KIND_DCP_PLRC)
+    return fail(GMES_ERR_VALUE, "unknown kind %d", p->kind);
+  if (p->npoints < 0 || p->nparam < 0 || p->nstate < 0 || p->npole < 0 || p->ncp < 0 ||
+      p->npole > GMES_MAX_POLES || p->ncp > GMES_MAX_POLES)
+    return fail(GMES_ERR_VALUE, "bad point-list sizes");
+  int need = 0, nstate = 0;
+  switch (p->kind) {
+    case GMES_KIND_DIELECTRIC: need = 1; break;
+    case GMES_KIND_CPML: need = 7; nstate = 2; break;
+    case GMES_KIND_UPML: need = 7; nstate = 1; break;
+    case GMES_KIND_DRUDE:
+    case GMES_KIND_LORENTZ: need = 3 * p->npole + 3; nstate = 2 * p->npole; break;
+    case GMES_KIND_DCP: need = 3 * p->npole + 5 * p->ncp + 4; nstate = 1 + 2 * p->npole + 2 * p->ncp; break;
+    case GMES_KIND_DCP_PLRC: need = 3 * p->npole + 6 * p->ncp + 3; nstate = p->npole + 2 * p->ncp; break;
+    case GMES_KIND_CONST: need = 1; break;
+    default: break;
+  }
+  if (p->nparam < need || p->nstate < nstate)
+    return fail(GMES_ERR_VALUE, "kind %d needs %d parameters and %d state slots per point",
+                p->kind, need, nstate);
+  if (p->npoints > 0 && (p->idx == nullptr || (p->nparam > 0 && p->param == nullptr) ||
+                         (p->nstate > 0 && p->state == nullptr)))
+    return fail(GMES_ERR_VALUE, "NULL point arrays");
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      if (p->shape[a][b] < 1) return fail(GMES_ERR_VALUE, "array extents must be >= 1");
+  if (p->kind == GMES_KIND_DUMMY || p->npoints == 0) return GMES_OK;
+  cudaError_t e = launch_points(*p, inplace, in1, in2, d1, d2, dt, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching the point-list kernel");
+  return GMES_OK;
+}
 
 // ---------------------------------------------------------------------------
 // gmes_batch_step_noalloc: the batch tables in a fixed device array.

@@ -171,6 +171,8 @@ __global__ void k_build_classes(gmes_grid_desc g, CoefLayout L) {
   cc.c2 = make_coef(cdt / d2);
   cc.reps = make_coef(1.0 / cd.eps);
   cc.value = make_coef(cd.kind == GMES_KIND_CONST && cd.nparam > 0 ? prm[cd.param_off] : 0.0);
+  cc.value_im =
+      make_coef(cd.kind == GMES_KIND_CONST && cd.nparam > 1 ? prm[cd.param_off + 1] : 0.0);
 
   const double* p = prm + cd.param_off;
   if (cd.kind == GMES_KIND_DRUDE || cd.kind == GMES_KIND_LORENTZ) {

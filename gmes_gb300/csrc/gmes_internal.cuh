@@ -45,7 +45,8 @@ struct ClassCoef {
   Coef c1;    // dt / eps / d1   (d1, d2: cell sizes of the two curl axes)
   Coef c2;    // dt / eps / d2
   Coef reps;  // 1 / eps
-  Coef value; // CONST
+  Coef value; // CONST (real part)
+  Coef value_im; // CONST, imaginary part (complex grids)
 };
 
 // Dispersive coefficients of one class: a[p][3] (Drude/Lorentz poles or DCP
@@ -161,6 +162,8 @@ struct GridDev {
   int32_t nprobe;
   int32_t pad3;
   double phase[6][2][2];   // Bloch phase factors (complex grids)
+  int32_t part;            // 0: real plane, 1: imaginary plane (complex grids)
+  int32_t pad4;
 };
 
 // Host-side launch plan of one grid: its real-plane view, the imaginary-
@@ -326,6 +329,9 @@ cudaError_t launch_tmz_adjoint(int precision, const GridDev& g, const TmzDev& t,
                                int nsteps, cudaStream_t s);
 cudaError_t launch_tmz_objective(const GridDev& g, const TmzDev& t, int nsteps, double* J,
                                  cudaStream_t s);
+
+cudaError_t launch_points(const gmes_points& g, void* inplace, const void* in1, const void* in2,
+                          double d1, double d2, double dt, cudaStream_t s);
 
 // Host-side helpers implemented in gmes_capi.cu.
 GridDev make_grid_dev(const gmes_grid_desc& g);

@@ -130,7 +130,7 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
     return;
   }
   if (kind == GMES_KIND_CONST) {
-    P::st(fp, P::cfg(&(cc.value)));
+    P::st(fp, P::cfg(g.part ? &(cc.value_im) : &(cc.value)));
     return;
   }
   if constexpr (DISP && E) {
@@ -289,7 +289,7 @@ __device__ __forceinline__ void update_strict(const GridDev& g, int64_t lin, con
     return;
   }
   if (kind == GMES_KIND_CONST) {
-    *fp = cc.value.d;
+    *fp = g.part ? cc.value_im.d : cc.value.d;
     return;
   }
   if constexpr (DISP && E) {

@@ -66,10 +66,20 @@ class ClassDesc:
         return f"ClassDesc({KIND_NAMES[self.kind]}, eps={self.eps}, params={self.params})"
 
 
+_PW_COMPS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+
+
 class Material:
-    """Base of the material types (src/pygeom.pyx:19-112)."""
+    """Base of the material types (src/pygeom.pyx:19-112).
+
+    ``get_pw_material_e?/h?(idx, coords, underneath=None, cmplx=False)``
+    return the reference's point-wise updater for one point (a
+    ``gmes_gb300.pw_material`` object, run on the GPU), with the point's
+    parameters filled as src/material.pyx does.
+    """
 
     compound = False
+    pw_model = None
 
     def __init__(self, eps_inf=1, mu_inf=1):
         self.eps_inf = float(eps_inf)
@@ -89,9 +99,50 @@ class Material:
     def engine_class(self, comp, underneath=None):
         raise NotImplementedError(f"{type(self).__name__} is not supported by the GPU engine")
 
+    # -- point-wise updaters (src/material.pyx get_pw_material_*) -----------
+    def _pw(self, c, idx, coords, underneath, cmplx):
+        from . import pw_material as pm
+        if self.pw_model is None:
+            raise NotImplementedError(f"{type(self).__name__} has no point-wise updater")
+        sfx = "Cmplx" if cmplx else "Real"
+        upd = getattr(pm, self.pw_model + _PW_COMPS[c] + sfx)()
+        param = getattr(pm, self.pw_model + ("Electric" if c < 3 else "Magnetic") + "Param"
+                        + sfx)()
+        src = self if underneath is None else underneath
+        if c < 3:
+            param.eps_inf = src.eps_inf
+        else:
+            param.mu_inf = src.mu_inf
+        self._fill_pw(param, c, coords)
+        upd.attach(idx, param)
+        return upd
+
+    def _fill_pw(self, param, c, coords):
+        pass
+
+    def get_pw_material_ex(self, idx, coords, underneath=None, cmplx=False):
+        return self._pw(0, idx, coords, underneath, cmplx)
+
+    def get_pw_material_ey(self, idx, coords, underneath=None, cmplx=False):
+        return self._pw(1, idx, coords, underneath, cmplx)
+
+    def get_pw_material_ez(self, idx, coords, underneath=None, cmplx=False):
+        return self._pw(2, idx, coords, underneath, cmplx)
+
+    def get_pw_material_hx(self, idx, coords, underneath=None, cmplx=False):
+        return self._pw(3, idx, coords, underneath, cmplx)
+
+    def get_pw_material_hy(self, idx, coords, underneath=None, cmplx=False):
+        return self._pw(4, idx, coords, underneath, cmplx)
+
+    def get_pw_material_hz(self, idx, coords, underneath=None, cmplx=False):
+        return self._pw(5, idx, coords, underneath, cmplx)
+
 
 class Dummy(Material):
     """No update: the point is only refreshed by the ghost-plane copy (src/pw_dummy.hh)."""
+
+    pw_model = "Dummy"
 
     def engine_class(self, comp, underneath=None):
         return ClassDesc(KIND_DUMMY, self._own(comp, underneath))
@@ -100,18 +151,27 @@ class Dummy(Material):
 class Const(Material):
     """Writes a constant value at every step (src/pw_const.hh)."""
 
+    pw_model = "Const"
+
     def __init__(self, value=0, eps_inf=1, mu_inf=1):
         super().__init__(eps_inf, mu_inf)
-        if isinstance(value, complex):
-            raise NotImplementedError("complex Const values need Bloch fields")
-        self.value = float(value)
+        self.value = complex(value) if isinstance(value, complex) else float(value)
 
     def engine_class(self, comp, underneath=None):
+        if isinstance(self.value, complex):
+            # the imaginary part is written on the imaginary plane of complex grids
+            return ClassDesc(KIND_CONST, self._own(comp, underneath),
+                             (self.value.real, self.value.imag))
         return ClassDesc(KIND_CONST, self._own(comp, underneath), (self.value,))
+
+    def _fill_pw(self, param, c, coords):
+        param.value = self.value
 
 
 class Dielectric(Material):
     """Non-dispersive isotropic medium (src/material.pyx:281-420, src/pw_dielectric.hh)."""
+
+    pw_model = "Dielectric"
 
     def engine_class(self, comp, underneath=None):
         return ClassDesc(KIND_DIELECTRIC, self._own(comp, underneath))
@@ -209,6 +269,17 @@ class Upml(Pml):
         s, k = self._sk(w, component)
         return 2 * k - s * self.dt
 
+    pw_model = "Upml"
+
+    def _fill_pw(self, param, c, coords):
+        own, a1, a2 = c % 3, (c % 3 + 1) % 3, (c % 3 + 2) % 3
+        param.c1 = self.c1(coords[a1], a1)
+        param.c2 = self.c2(coords[a1], a1)
+        param.c3 = self.c3(coords[a2], a2)
+        param.c4 = self.c4(coords[a2], a2)
+        param.c5 = self.c5(coords[own], own)
+        param.c6 = self.c6(coords[own], own)
+
     def engine_class(self, comp, underneath=None):
         return ClassDesc(KIND_UPML, self._own(comp, underneath), pml=self)
 
@@ -243,6 +314,17 @@ class Cpml(Pml):
         denominator = (sigma + kappa * self.a(w, component)) * kappa
         return numerator / denominator if denominator else 0
 
+    pw_model = "Cpml"
+
+    def _fill_pw(self, param, c, coords):
+        a1, a2 = (c % 3 + 1) % 3, (c % 3 + 2) % 3
+        param.b1 = self.b(coords[a1], a1)
+        param.b2 = self.b(coords[a2], a2)
+        param.c1 = self.c(coords[a1], a1)
+        param.c2 = self.c(coords[a2], a2)
+        param.kappa1 = self.kappa(coords[a1], a1)
+        param.kappa2 = self.kappa(coords[a2], a2)
+
     def engine_class(self, comp, underneath=None):
         return ClassDesc(KIND_CPML, self._own(comp, underneath), pml=self)
 
@@ -270,6 +352,12 @@ class CriticalPoint:
 
 class Drude(Dielectric):
     """Drude ADE medium (src/material.pyx:1500-1660, src/pw_drude.hh)."""
+
+    pw_model = "Drude"
+
+    def _fill_pw(self, param, c, coords):
+        if c < 3:
+            param.set(self.a, self.c)
 
     def __init__(self, eps_inf=1, mu_inf=1, sigma=0, dps=()):
         super().__init__(eps_inf, mu_inf)
@@ -305,6 +393,12 @@ class Drude(Dielectric):
 class Lorentz(Dielectric):
     """Lorentz ADE medium (src/material.pyx:1663-1858, src/pw_lorentz.hh)."""
 
+    pw_model = "Lorentz"
+
+    def _fill_pw(self, param, c, coords):
+        if c < 3:
+            param.set(self.a, self.c)
+
     def __init__(self, eps_inf=1, mu_inf=1, sigma=0, lps=()):
         super().__init__(eps_inf, mu_inf)
         self.sigma = float(sigma)
@@ -338,6 +432,12 @@ class Lorentz(Dielectric):
 
 class DcpAde(Dielectric):
     """Drude-critical-points medium, ADE form (src/material.pyx:1029-1176, src/pw_dcp.hh:44-400)."""
+
+    pw_model = "DcpAde"
+
+    def _fill_pw(self, param, c, coords):
+        if c < 3:
+            param.set(self.a, self.b, self.c)
 
     def __init__(self, eps_inf=1, mu_inf=1, sigma=0, dps=(), cps=()):
         super().__init__(eps_inf, mu_inf)
@@ -409,6 +509,12 @@ class DcpPlrc(Dielectric):
     recomputes them in FP64 on the GPU from the physical parameters and the
     transcendental values taken here with the host libm.
     """
+
+    pw_model = "DcpPlrc"
+
+    def _fill_pw(self, param, c, coords):
+        if c < 3:
+            param.set(self.a, self.b, self.c)
 
     rc = False
 

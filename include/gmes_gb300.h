@@ -98,7 +98,7 @@ enum { GMES_EX = 0, GMES_EY = 1, GMES_EZ = 2, GMES_HX = 3, GMES_HY = 4, GMES_HZ 
  * (replaces the per-point <Model>ElectricParam / MagneticParam structs,
  * src/pw_material.i:215-348).  Parameters live in a double pool:
  *   DIELECTRIC, CPML, UPML, DUMMY: none
- *   CONST:   value
+ *   CONST:   value (complex grids: value, imaginary part)
  *   DRUDE:   eps_inf, sigma, then (omega, gamma) per pole   (src/material.pyx:1546-1565)
  *   LORENTZ: eps_inf, sigma, then (amp, omega, gamma) per pole (src/material.pyx:1727-1746)
  *   DCP:     eps_inf, sigma, (omega, gamma) per Drude term,
@@ -483,6 +483,44 @@ gmes_status gmes_tmz_objective(const gmes_grid_desc* g, const gmes_tmz_batch* b,
    GMES_TMZ_RECORD_HIST from the state after step0). */
 gmes_status gmes_tmz_adjoint(const gmes_grid_desc* g, const gmes_tmz_batch* b, int32_t step0,
                              int32_t nsteps, void* stream);
+
+/*
+ * Point-list updaters: the reference's PwMaterial operator objects
+ * (<Model><Comp><Real|Cmplx>.update_all, src/pw_material.hh:66-73,
+ * src/pw_material.i:138-389).  One call updates the attached points of one
+ * updater in place, in the reference's operation order (FP64), reading the
+ * two curl inputs with its field_at() collapsed-axis rule.  All pointers are
+ * device memory; complex updaters (cmplx = 1) take planar arrays (real plane
+ * then imaginary plane) and two planes of param and state.
+ * Per-point param layouts (doubles) and state slots:
+ *   DIELECTRIC: eps                                  state: -
+ *   CPML:  eps, b1, b2, c1, c2, kappa1, kappa2       state: psi1, psi2
+ *   UPML:  eps, c1, c2, c3, c4, c5, c6               state: d (E) / b (H)
+ *   DRUDE, LORENTZ: a[npole][3], c[3]                state: q_now[npole], q_new[npole]
+ *   DCP:   a[npole][3], b[ncp][5], c[4]              state: e_old, q_old, q_now, p_old, p_now
+ *   DCP_PLRC: a[npole][3], b[ncp][6] (re/im of b0, b1, b2), c[3]
+ *                                                    state: psi_dp[npole], psi_cp[ncp][2]
+ *   CONST: value                                     state: -
+ * Points outside the target array are skipped (the reference raises
+ * IndexError before any write; its Python binding checks, as this
+ * package's binding does).
+ */
+typedef struct {
+  int32_t comp;          /* field component 0..5 of the target */
+  int32_t kind;          /* gmes_kind */
+  int32_t npoints;
+  int32_t nparam;        /* doubles per point */
+  int32_t nstate;        /* state slots per point */
+  int32_t npole, ncp;
+  int32_t cmplx;
+  const int32_t* idx;    /* [npoints][3] */
+  const double* param;   /* [planes][npoints][nparam] */
+  double* state;         /* [planes][npoints][nstate] */
+  int64_t shape[3][3];   /* shapes of the target and the two inputs */
+} gmes_points;
+
+gmes_status gmes_points_update(const gmes_points* p, void* inplace, const void* in1,
+                               const void* in2, double d1, double d2, double dt, void* stream);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char* gmes_last_error(void);

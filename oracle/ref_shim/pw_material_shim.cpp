@@ -23,6 +23,7 @@
 
 #include "pw_material.hh"
 #include "pw_dummy.hh"
+#include "pw_const.hh"
 #include "pw_dielectric.hh"
 #include "pw_upml.hh"
 #include "pw_cpml.hh"
@@ -71,18 +72,22 @@ template <typename T, typename Cls>
 void def_updater_methods(Cls& cls) {
   using C = typename Cls::type;
   cls.def(py::init<>())
+      // attach/merge return the updater itself, as the SWIG binding's
+      // PwMaterial<T>* results do (src/pw_material.hh:60-74)
       .def("attach",
-           [](C& self, py::handle idx, const PwMaterialParam& p) {
+           [](C& self, py::handle idx, const PwMaterialParam& p) -> C& {
              const auto v = as_index(idx);
              try {
                static_cast<PwMaterial<T>&>(self).attach(v.data(), static_cast<int>(v.size()), &p);
              } catch (const std::invalid_argument& e) {
                throw py::value_error(e.what());
              }
-           })
-      .def("merge", [](C& self, const C& other) {
+             return self;
+           }, py::return_value_policy::reference)
+      .def("merge", [](C& self, const C& other) -> C& {
         static_cast<PwMaterial<T>&>(self).merge(&other);
-      })
+        return self;
+      }, py::return_value_policy::reference)
       .def("update_all",
            [](C& self, py::array inplace, py::array in1, py::array in2, double d1,
               double d2, double dt, double n) {
@@ -154,6 +159,20 @@ void bind_all(py::module_& m, const std::string& sfx) {
   def_magnetic<T, DummyHx>(m, "DummyHx" + sfx);
   def_magnetic<T, DummyHy>(m, "DummyHy" + sfx);
   def_magnetic<T, DummyHz>(m, "DummyHz" + sfx);
+
+  // Const
+  py::class_<ConstElectricParam<T>, ElectricParam<T>>(m, ("ConstElectricParam" + sfx).c_str())
+      .def(py::init<>())
+      .def_readwrite("value", &ConstElectricParam<T>::value);
+  py::class_<ConstMagneticParam<T>, MagneticParam<T>>(m, ("ConstMagneticParam" + sfx).c_str())
+      .def(py::init<>())
+      .def_readwrite("value", &ConstMagneticParam<T>::value);
+  def_electric<T, ConstEx>(m, "ConstEx" + sfx);
+  def_electric<T, ConstEy>(m, "ConstEy" + sfx);
+  def_electric<T, ConstEz>(m, "ConstEz" + sfx);
+  def_magnetic<T, ConstHx>(m, "ConstHx" + sfx);
+  def_magnetic<T, ConstHy>(m, "ConstHy" + sfx);
+  def_magnetic<T, ConstHz>(m, "ConstHz" + sfx);
 
   // Dielectric
   py::class_<DielectricElectricParam<T>, ElectricParam<T>>(

@@ -260,6 +260,88 @@ CASES = {
     "dcp_plrc_bloch2d": dcp_plrc_bloch2d,
 }
 
+# ---------------------------------------------------------------------------
+# Point-wise updaters (the reference's gmes.pw_material objects)
+# ---------------------------------------------------------------------------
+PW_MODELS = ("Dummy", "Const", "Dielectric", "Upml", "Cpml", "Drude", "Lorentz", "DcpAde",
+             "DcpPlrc", "DcpRc")
+PW_COMPS = ("ex", "ey", "ez", "hx", "hy", "hz")
+PW_POINTS = ((1, 1, 1), (2, 1, 2), (1, 2, 1))
+PW_SHAPE = (4, 4, 4)
+PW_STEPS = 3
+
+
+def pw_material(g, model):
+    """A material of each point-wise model, initialised as FDTD.init would."""
+    space = g.Cartesian((0, 0, 0))
+    space.dt = 0.35
+    rng = np.random.default_rng(5)
+    cps = tuple(g.CriticalPoint(amp=float(rng.uniform(0.5, 2.0)), phi=float(rng.uniform(-1, 1)),
+                                omega=float(rng.uniform(2.0, 5.0)),
+                                gamma=float(rng.uniform(0.2, 1.0))) for _ in range(2))
+    if model == "Dummy":
+        m = g.Dummy(eps_inf=2.0, mu_inf=1.5)
+    elif model == "Const":
+        m = g.Const(value=0.75, eps_inf=2.5, mu_inf=1.25)
+    elif model == "Dielectric":
+        m = g.Dielectric(eps_inf=2.5, mu_inf=1.25)
+    elif model in ("Upml", "Cpml"):
+        m = g.Upml() if model == "Upml" else g.Cpml()
+        m.init(space, ((0, 0, 0), (1.0, 1.0, 1.0), 0.6))
+        return m
+    elif model == "Drude":
+        m = g.Drude(eps_inf=1.5, sigma=0.05, dps=(g.DrudePole(omega=3.0, gamma=0.3),
+                                                 g.DrudePole(omega=1.0, gamma=0.1)))
+    elif model == "Lorentz":
+        m = g.Lorentz(eps_inf=1.2, lps=(g.LorentzPole(amp=2.0, omega=3.0, gamma=0.1),))
+    elif model == "DcpAde":
+        m = g.DcpAde(eps_inf=1.1, dps=(g.DrudePole(omega=7.0, gamma=0.2),), cps=cps)
+    elif model == "DcpPlrc":
+        m = g.DcpPlrc(eps_inf=1.1, dps=(g.DrudePole(omega=7.0, gamma=0.2),), cps=cps)
+    else:
+        m = g.DcpRc(eps_inf=1.3, sigma=0.1, dps=(g.DrudePole(omega=4.0, gamma=0.5),),
+                    cps=cps[:1])
+    m.init(space)
+    return m
+
+
+def pw_updater(g, model, comp, cmplx):
+    """An updater with PW_POINTS attached (merged one point at a time)."""
+    m = pw_material(g, model)
+    get = getattr(m, "get_pw_material_" + comp)
+    upd = None
+    for q, idx in enumerate(PW_POINTS):
+        coords = (0.55 + 0.1 * q, -0.7 + 0.05 * q, 0.8 - 0.1 * q)
+        u = get(idx, coords, cmplx=cmplx)
+        upd = u if upd is None else upd.merge(u)
+    return upd
+
+
+def pw_inputs(model, comp, cmplx, step):
+    """Seeded inplace, in1, in2 arrays of one update_all call."""
+    seed = (PW_MODELS.index(model) * 6 + PW_COMPS.index(comp)) * 2 + int(cmplx)
+    rng = np.random.default_rng(1000 + 10 * seed + step)
+
+    def arr():
+        a = rng.standard_normal(PW_SHAPE)
+        if cmplx:
+            a = a + 1j * rng.standard_normal(PW_SHAPE)
+        return np.ascontiguousarray(a)
+    return arr(), arr(), arr()
+
+
+def pw_run(g, model, comp, cmplx):
+    """The target array after each of PW_STEPS update_all calls (state carried)."""
+    upd = pw_updater(g, model, comp, cmplx)
+    target = pw_inputs(model, comp, cmplx, 0)[0]
+    out = []
+    for step in range(PW_STEPS):
+        _, in1, in2 = pw_inputs(model, comp, cmplx, step)
+        upd.update_all(target, in1, in2, 0.4, 0.3, 0.35, step)
+        out.append(target.copy())
+    return np.stack(out)
+
+
 # Cases whose golden file stores only Ez in full (and checksums of the rest)
 # to keep the fixture small.
 SUMMARY_ONLY = {"air2d": ("ez",)}

@@ -8,6 +8,7 @@ these files; they never need the reference itself.
 
 Usage:  python tests/golden/make_golden.py [case ...]
         python tests/golden/make_golden.py --probes [case ...]
+        python tests/golden/make_golden.py --pw
 """
 
 import json
@@ -93,9 +94,26 @@ def probes(names):
                 print("probe", name, comp, flush=True)
 
 
+def pw_updaters():
+    """Every point-wise updater of the reference on seeded arrays -> pw_updaters.npz."""
+    from cases import PW_COMPS, PW_MODELS, pw_run
+    from oracle.refpkg import load_reference
+    gmes = load_reference()
+    out = {}
+    for model in PW_MODELS:
+        for comp in PW_COMPS:
+            for cmplx in (False, True):
+                key = f"{model}_{comp}_{'C' if cmplx else 'R'}"
+                out[key] = pw_run(gmes, model, comp, cmplx)
+    np.savez_compressed(HERE / "pw_updaters.npz", **out)
+    print("pw_updaters:", len(out), "updaters", flush=True)
+
+
 if __name__ == "__main__":
     args = sys.argv[1:]
-    if args[:1] == ["--probes"]:
+    if args[:1] == ["--pw"]:
+        pw_updaters()
+    elif args[:1] == ["--probes"]:
         probes(args[1:] or list(PROBES))
     else:
         main(args or list(CASES))
