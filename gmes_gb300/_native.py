@@ -5,10 +5,14 @@ loudly when the library is missing: the package has no CPU fallback.
 """
 
 import ctypes as C
+import os
 from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
-LIB_PATH = PKG / "libgmes_gb300.so"
+# GMES_GB300_LIB selects another build of the library (e.g. one compiled
+# with different tuning macros); the default is the in-tree build.
+LIB_PATH = Path(os.environ["GMES_GB300_LIB"]) if os.environ.get("GMES_GB300_LIB") else \
+    PKG / "libgmes_gb300.so"
 
 ABI_VERSION = 4
 MAX_CLASSES = 256
@@ -135,6 +139,8 @@ def load():
     if _lib is not None:
         return _lib
     if not LIB_PATH.exists():
+        if os.environ.get("GMES_GB300_LIB"):
+            raise RuntimeError(f"GMES_GB300_LIB={LIB_PATH} does not exist")
         from . import build as _build
         _build.build()
     lib = C.CDLL(str(LIB_PATH))
