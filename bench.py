@@ -327,8 +327,7 @@ def run_ours(args):
     peak, peak_src = measured_peak()
     achieved = dom[1] / (dom[2] / 1e3) / 1e9
     step_bytes = eb + hb
-    key = f"{cfg['workload']}/{args.precision}"
-    traffic = ncu_traffic(key, args.precision)
+    traffic = ncu_traffic(cfg["workload"], args.precision)
     result = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5),

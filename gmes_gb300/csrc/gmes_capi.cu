@@ -547,6 +547,10 @@ gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs
       return fail(GMES_ERR_VALUE, "grid %d: all grids of a batch must share one precision", q);
     disp = disp || (g->flags & GMES_FLAG_DISPERSIVE);
     jobs[q] = make_grid_dev(*g);
+    if (!offsets_fit_i32(jobs[q]))
+      return fail(GMES_ERR_VALUE,
+                  "grid %d has a component of 2^31 or more points: step it alone, not in a batch",
+                  q);
     int l = 0;
     while (l < bx_cap && (1 << l) < g->n[2]) ++l;
     bxl[q] = l;
@@ -1061,6 +1065,10 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
       return fail(GMES_ERR_VALUE, "steps[%d] exceeds the grid's source-value capacity", q);
     disp = disp || (g->flags & GMES_FLAG_DISPERSIVE);
     jobs[q] = make_grid_dev(*g);
+    if (!offsets_fit_i32(jobs[q]))
+      return fail(GMES_ERR_VALUE,
+                  "grid %d has a component of 2^31 or more points: step it alone, not in a batch",
+                  q);
     int l = 0;
     while (l < bx_cap && (1 << l) < g->n[2]) ++l;
     bxl[q] = l;

@@ -275,6 +275,14 @@ __device__ __forceinline__ double to_double(df v) { return (double)v.hi + (doubl
 constexpr int kBatchThreads = 256;
 
 // Kernel-side view of a batch workspace (gmes_batch_prepare).
+// True when every component of the grid holds fewer than 2^31 points, so
+// the cell kernels may index it with 32-bit offsets.
+inline bool offsets_fit_i32(const GridDev& d) {
+  for (int c = 0; c < 6; ++c)
+    if (d.npts[c] >= (int64_t(1) << 31)) return false;
+  return true;
+}
+
 struct BatchView {
   const GridDev* jobs;
   const int64_t* tile_prefix;   // [njobs + 1] blocks of each grid's half-step

@@ -444,7 +444,8 @@ __device__ __forceinline__ Pre<P> pre_of(const GridDev& g, int64_t lin, const in
 }
 
 // MASK: the active-component mask when known at compile time, 0 when read
-// from the grid; I: offset type.  (Only <0, int64_t> is instantiated.)
+// from the grid; I: offset type (int32_t for grids whose components hold
+// fewer than 2^31 points, int64_t otherwise).
 template <class P, int SIDE, bool STRICT, bool DISP, int MASK, class I>
 __device__ __forceinline__ void cell_body(const GridDev& g, int i, int j, int k) {
   using R = typename P::R;
@@ -760,7 +761,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_multi_cell(const Batch
     const int jb = rem / nkb, kb = rem - jb * nkb;
     const int k = kb * bx + (threadIdx.x & (bx - 1));
     const int j = jb * by + (threadIdx.x >> bxl);
-    if (k < g.n[2] && j < g.n[1]) cell_body<P, SIDE, STRICT, DISP, 0, int64_t>(g, i, j, k);
+    // batched grids hold fewer than 2^31 points per component (checked when
+    // the batch is prepared)
+    if (k < g.n[2] && j < g.n[1]) cell_body<P, SIDE, STRICT, DISP, 0, int32_t>(g, i, j, k);
   }
 }
 
@@ -821,11 +824,15 @@ void run_half(const Plan& p, int side, int st, cudaStream_t s) {
     for (int i0 = 0; i0 < d.n[0]; i0 += kMaxY) {
       const dim3 grid((unsigned)((d.n[2] + bx - 1) / bx), (unsigned)((d.n[1] + by - 1) / by),
                       (unsigned)min(kMaxY, d.n[0] - i0));
-      // Measured on GB300: a compile-time active mask (all six components) or
-      // 32-bit offsets do not speed this kernel up -- the full-mask variant
-      // ran ~35% slower at 256^3 -- so one runtime-mask, 64-bit-offset
-      // instantiation serves every grid.
-      launch_cell<P, STRICT, 0, int64_t>(v, side, p.disp, grid, bx_log2, i0, s);
+      // Measured on GB300 (256^3 cube): 32-bit offsets run the FP64 step 7%
+      // and the df64 step 6% faster than 64-bit ones (fewer registers and
+      // spills), so every grid whose components hold fewer than 2^31 points
+      // takes them; a compile-time active mask (all six components) ran ~35%
+      // slower, so the mask stays a runtime value.
+      if (offsets_fit_i32(d))
+        launch_cell<P, STRICT, 0, int32_t>(v, side, p.disp, grid, bx_log2, i0, s);
+      else
+        launch_cell<P, STRICT, 0, int64_t>(v, side, p.disp, grid, bx_log2, i0, s);
     }
   }
   for (int part = 0; part < nplanes; ++part) {
