@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--workload", choices=("cube", "dispersive", "air2d", "serving", "design2d"),
                     default="cube")
     ap.add_argument("--batch", type=int, default=64, help="design2d: designs per gradient call")
+    ap.add_argument("--block-steps", type=int, default=0,
+                    help="design2d, fp32: steps per kernel launch (0: temporally blocked "
+                         "default, 1: one step per launch)")
     ap.add_argument("--jobs", type=int, default=64, help="serving: number of jobs")
     ap.add_argument("--rate", type=float, default=0.0,
                     help="serving: Poisson arrival rate in jobs/s (0: all at t = 0)")
@@ -477,7 +480,7 @@ def run_design(args):
     n = args.n or 512
     space, geom, src, design, monitor, eps, nsteps = W.design2d(n=n, batch=args.batch)
     prob = TMzAdjoint(space, geom, src, design, monitor, nsteps, batch=args.batch,
-                      precision=precision)
+                      precision=precision, block_steps=args.block_steps)
     cells = n * n
     x = torch.tensor(eps, dtype=torch.float64, device="cuda")
     for _ in range(max(1, args.warmup)):
@@ -522,7 +525,7 @@ def run_design(args):
                    "design_points": [64, 64], "monitor_points": [8, 8], "time_steps": nsteps,
                    "batch": args.batch, "checkpoint_segment": prob.segment,
                    "checkpoints": (nsteps + prob.segment - 1) // prob.segment,
-                   "precision": precision,
+                   "precision": precision, "block_steps": args.block_steps,
                    "l2": "state 7 x batch x n^2 x elem > L2 for batch 64 (inputs larger than L2)"},
         "gradients_per_s": round(args.batch / per, 3),
         "forward_s": round(tf, 4), "backward_s": round(tb, 4),
@@ -530,15 +533,27 @@ def run_design(args):
         "hbm_peak_GBps": peak[0] if peak else None,
         "wall_s": round(wall, 3), "grad_finite": bool(torch.isfinite(g).all()),
         "clocks": clocks,
-        # forward: 4 launches per step (E, E sources, H, H sources); backward:
-        # the recompute (4 per step) and the adjoint (4 per step); + design
-        # and objective
-        "gpu_launches": args.steps * (12 * nsteps + 2),
+        "gpu_launches": args.steps * (design_launches(prob, precision, args.block_steps) + 2),
     }
     if not args.no_cpu_baseline:
         result["cpu_baseline"] = design_cpu_baseline(space, geom, src, design, monitor, eps,
                                                      prob, n)
     print(json.dumps(result), flush=True)
+
+
+def design_launches(prob, precision, block_steps, max_block_steps=4):
+    """Kernel launches of one forward + backward (recompute and adjoint).
+
+    One step per launch: E, E sources, H, H sources per step in each of the
+    three passes.  FP32 temporally blocked (block_steps 0 = the library's
+    most, 4): one launch per block of steps of each checkpoint segment.
+    """
+    nsteps, seg = prob.nsteps, prob.segment
+    per = (block_steps or max_block_steps) if precision == "fp32" else 1
+    if per == 1:
+        return 12 * nsteps
+    segs = [min(seg, nsteps - s0) for s0 in range(0, nsteps, seg)]
+    return 3 * sum((k + per - 1) // per for k in segs)
 
 
 def design_cpu_baseline(space, geom, src, design, monitor, eps, prob, n, steps=100):

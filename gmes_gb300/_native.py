@@ -14,7 +14,7 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ["GMES_GB300_LIB"]) if os.environ.get("GMES_GB300_LIB") else \
     PKG / "libgmes_gb300.so"
 
-ABI_VERSION = 4
+ABI_VERSION = 5
 MAX_CLASSES = 256
 MAX_PML = 4
 MAX_POLES = 8
@@ -111,9 +111,11 @@ class TmzBatchC(C.Structure):
     _fields_ = [("nbatch", C.c_int32), ("design_lo", C.c_int32 * 2), ("design_n", C.c_int32 * 2),
                 ("monitor_lo", C.c_int32 * 2), ("monitor_n", C.c_int32 * 2),
                 ("nsrc", C.c_int32), ("total_steps", C.c_int32), ("hist_steps", C.c_int32),
+                ("block_steps", C.c_int32),
                 ("state", C.c_void_p), ("adjoint", C.c_void_p), ("design", C.c_void_p),
                 ("hist", C.c_void_p), ("monitor", C.c_void_p), ("grad", C.c_void_p),
-                ("weight", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p)]
+                ("weight", C.c_void_p), ("src", C.c_void_p), ("src_val", C.c_void_p),
+                ("scratch", C.c_void_p)]
 
 
 class PointsC(C.Structure):

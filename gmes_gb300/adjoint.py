@@ -83,10 +83,14 @@ class TMzAdjoint:
     materials; the design region must lie on dielectric Ez points.
     ``precision``: "fp32" (FP32 fields and adjoint, FP64-derived
     coefficients, FP64 gradient accumulation), "fp64" or "df64".
+    ``block_steps``: FP32 steps per kernel launch (0: the most the
+    temporally blocked kernels take, 1: one step per launch); every value
+    gives bit-identical fields and gradients.
     """
 
     def __init__(self, space, geom_list, src_list, design, monitor, nsteps, batch=1,
-                 precision="fp32", segment=None, courant_ratio=0.99, dt=None, device=None):
+                 precision="fp32", segment=None, courant_ratio=0.99, dt=None, device=None,
+                 block_steps=0):
         from .fdtd import TMzFDTD
         torch = _torch()
         if precision not in ("fp32", "fp64", "df64"):
@@ -119,7 +123,8 @@ class TMzAdjoint:
         b.nsrc = len(rows)
         b.total_steps = self.nsteps
         b.hist_steps = self.segment
-        sizes = (C.c_int64 * 6)()
+        b.block_steps = int(block_steps)
+        sizes = (C.c_int64 * 7)()
         N.check(self.lib.gmes_tmz_sizes(C.byref(self.grid.desc), C.byref(b), sizes))
         self.sizes = list(sizes)
         dev = self.device
@@ -133,6 +138,7 @@ class TMzAdjoint:
         self.hist = buf(sizes[3])
         self.monitor = buf(sizes[4])
         self.grad = buf(sizes[5])
+        self.scratch = buf(sizes[6]) if sizes[6] > 0 else None
         nd, nb = dn[0] * dn[1], self.batch
         self.eps = torch.ones((nb, nd), dtype=torch.float64, device=dev)
         self.weight = torch.ones(nb, dtype=torch.float64, device=dev)
@@ -151,6 +157,7 @@ class TMzAdjoint:
         b.hist = self.hist.data_ptr()
         b.monitor = self.monitor.data_ptr()
         b.grad = self.grad.data_ptr()
+        b.scratch = self.scratch.data_ptr() if self.scratch is not None else None
         b.weight = self.weight.data_ptr()
         self.desc = b
         self.checkpoints = None  # (segments, state bytes), allocated by the first forward

@@ -23,8 +23,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           f"-I{ROOT / 'include'}"]
 # Per-file flags: the coefficient builder and the rasteriser reproduce the
-# reference's FP64 operation order, so multiply-add contraction is disabled.
-EXTRA = {"gmes_coef.cu": ["--fmad=false"], "gmes_raster.cu": ["--fmad=false"]}
+# reference's FP64 operation order, so multiply-add contraction is disabled;
+# the differentiation kernels write every fused multiply-add explicitly so
+# that their one-step and temporally blocked forms round alike.
+EXTRA = {"gmes_coef.cu": ["--fmad=false"], "gmes_raster.cu": ["--fmad=false"],
+         "gmes_adjoint.cu": ["--fmad=false"]}
 SOURCES = ["gmes_capi.cu", "gmes_coef.cu", "gmes_step.cu", "gmes_raster.cu", "gmes_adjoint.cu",
            "gmes_points.cu"]
 

@@ -34,12 +34,43 @@
 //   dJ/deps_p = sum_n lambda_E'(p) * dE'/deps_p = -1/eps_p sum_n lambda_E'(p) inc_p(n)
 // with inc_p(n) = c1 D1 - c2 D2 of forward step n, recorded when the step
 // is recomputed from a checkpoint.
+//
+// Resolved map.  Every lattice point's update is resolved once per design
+// set (k_tmz_map): most points (dielectric, design pixels, CPML outside
+// both profiles) update as F + c1 D1 + c2 D2 with two coefficients that
+// the kernels read from a small per-point map shared by the batch (L2
+// resident) instead of following class map -> class table -> profile
+// look-ups every step; CPML points inside a profile go through the
+// per-point functions below.
+//
+// Two kernel forms.  The one-step kernels advance every lattice point by
+// one half-step per launch.  The temporally blocked kernels (FP32) advance
+// a tile of one design by up to kTbHalo steps per launch from a region of
+// shared memory (see k_tmz_tb_fwd).  Both use the same map and per-point
+// functions, and this file is compiled without implicit multiply-add
+// contraction (every fused operation is an explicit fmadd), so the two
+// forms give bit-identical fields, adjoints and gradients.
 #include "gmes_internal.cuh"
 
 namespace gmes {
 namespace {
 
 constexpr int kBX = 32, kBY = 8;
+
+// a + b * c: one rounding in FP32 and FP64, the float-float operators for
+// the df type.
+template <class R>
+__device__ __forceinline__ R fmadd(R a, R b, R c) {
+  return a + b * c;
+}
+template <>
+__device__ __forceinline__ float fmadd<float>(float a, float b, float c) {
+  return __fmaf_rn(b, c, a);
+}
+template <>
+__device__ __forceinline__ double fmadd<double>(double a, double b, double c) {
+  return __fma_rn(b, c, a);
+}
 
 struct Lat {
   int i, j, b;
@@ -98,7 +129,357 @@ __device__ __forceinline__ Prof prof_y(const GridDev& g, int pm, int i, int j) {
 }
 
 // ---------------------------------------------------------------------------
-// Forward.
+// Per-point forward updates.
+// ---------------------------------------------------------------------------
+// New Ez of lattice point (i, j) of design b from its value e and curl
+// differences D1 = Y(i,j) - Y(i-1,j), D2 = X(i,j) - X(i,j-1): design pixels
+// with the design's own c1, c2, other points with their Dielectric or CPML
+// updater (other classes keep e).  s1, s2 point at the point's two psi
+// values, read and written only where their CPML profile is on.  *dp gets
+// the design index (-1 off the design) and, on design pixels, *inc the
+// increment c1 D1 - c2 D2.
+template <class P>
+__device__ __forceinline__ typename P::R e_point(const GridDev& g, const TmzDev& t, int b, int i,
+                                                 int j, typename P::R e, typename P::R D1,
+                                                 typename P::R D2, typename P::T* s1,
+                                                 typename P::T* s2, int64_t* dp,
+                                                 typename P::R* inc) {
+  using R = typename P::R;
+  const int64_t d = design_index(t, i, j);
+  *dp = d;
+  if (d >= 0) {
+    const DesignCoef* dc = t.dc + (int64_t)b * t.dn[0] * t.dn[1] + d;
+    const R c1 = P::cfg(&dc->c1), c2 = P::cfg(&dc->c2);
+    *inc = fmadd(-(c2 * D2), c1, D1);
+    return fmadd(fmadd(e, c1, D1), -c2, D2);
+  }
+  const ClassCoef& cc = class_e(g, i, j);
+  const int kind = __ldg(&cc.kind);
+  if (kind == GMES_KIND_DIELECTRIC)
+    return fmadd(fmadd(e, P::cfg(&cc.c1), D1), -P::cfg(&cc.c2), D2);
+  if (kind != GMES_KIND_CPML) return e;
+  const Prof q = prof_e(g, __ldg(&cc.pml), i, j);
+  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
+  if (!on1 && !on2) return fmadd(fmadd(e, P::cfg(&cc.c1), D1), -P::cfg(&cc.c2), D2);
+  R psi1 = P::ldw(s1), psi2 = P::ldw(s2);
+  if (on1) {
+    psi1 = fmadd(P::cfg(q.q1) * psi1, P::cfg(q.q1 + 3), D1);
+    P::st(s1, psi1);
+  }
+  if (on2) {
+    psi2 = fmadd(P::cfg(q.q2) * psi2, P::cfg(q.q2 + 3), D2);
+    P::st(s2, psi2);
+  }
+  const R xv = fmadd(fmadd(psi1 - psi2, P::cfg(q.q1 + 4), D1), -P::cfg(q.q2 + 4), D2);
+  return fmadd(e, P::cfg(&cc.cdt), xv);
+}
+
+// New Hx of lattice point (i, j) from its value x and D1 = E(i,j+1) - E(i,j);
+// s: its psi.
+template <class P>
+__device__ __forceinline__ typename P::R x_point(const GridDev& g, int i, int j, typename P::R x,
+                                                 typename P::R dx, typename P::T* s) {
+  using R = typename P::R;
+  const ClassCoef& cc = class_x(g, i, j);
+  const int kind = __ldg(&cc.kind);
+  if (kind == GMES_KIND_DIELECTRIC) return fmadd(x, -P::cfg(&cc.c1), dx);
+  if (kind != GMES_KIND_CPML) return x;
+  const Prof q = prof_x(g, __ldg(&cc.pml), i, j);
+  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
+  if (!on1 && !on2) return fmadd(x, -P::cfg(&cc.c1), dx);
+  R psi = P::ldw(s);
+  if (on1) {
+    psi = fmadd(P::cfg(q.q1) * psi, P::cfg(q.q1 + 3), dx);
+    P::st(s, psi);
+  }
+  return fmadd(x, -P::cfg(&cc.cdt), fmadd(psi, P::cfg(q.q1 + 4), dx));
+}
+
+// New Hy of lattice point (i, j) from its value y and D2 = E(i+1,j) - E(i,j);
+// s: its psi.
+template <class P>
+__device__ __forceinline__ typename P::R y_point(const GridDev& g, int i, int j, typename P::R y,
+                                                 typename P::R dy, typename P::T* s) {
+  using R = typename P::R;
+  const ClassCoef& cc = class_y(g, i, j);
+  const int kind = __ldg(&cc.kind);
+  if (kind == GMES_KIND_DIELECTRIC) return fmadd(y, P::cfg(&cc.c2), dy);
+  if (kind != GMES_KIND_CPML) return y;
+  const Prof q = prof_y(g, __ldg(&cc.pml), i, j);
+  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
+  if (!on1 && !on2) return fmadd(y, P::cfg(&cc.c2), dy);
+  R psi = P::ldw(s);
+  if (on2) {
+    psi = fmadd(P::cfg(q.q2) * psi, P::cfg(q.q2 + 3), dy);
+    P::st(s, psi);
+  }
+  return fmadd(y, -P::cfg(&cc.cdt), fmadd(-psi, -P::cfg(q.q2 + 4), dy));
+}
+
+// ---------------------------------------------------------------------------
+// Per-point adjoint curl weights.
+// ---------------------------------------------------------------------------
+// Curl weight of the Hx point (i, j): lambda_D1 = dX'/dD1 applied to its
+// adjoint *lxp, with D1 = E(i, j+1) - E(i, j).  phr: its psi adjoint before
+// this step; OWN: the advanced psi adjoint is written to *phw.
+template <class P, bool OWN>
+__device__ __forceinline__ typename P::R adj_x(const GridDev& g, int i, int j,
+                                               const typename P::T* lxp,
+                                               const typename P::T* phr, typename P::T* phw) {
+  using R = typename P::R;
+  const ClassCoef& cc = class_x(g, i, j);
+  const int kind = __ldg(&cc.kind);
+  if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return P::zero();
+  const R lx = P::ldw(lxp);
+  if (kind == GMES_KIND_DIELECTRIC) return -(P::cfg(&cc.c1) * lx);
+  const Prof q = prof_x(g, __ldg(&cc.pml), i, j);
+  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
+  if (!on1 && !on2) return -(P::cfg(&cc.c1) * lx);
+  const R cdt = P::cfg(&cc.cdt);
+  const R direct = -(cdt * (P::cfg(q.q1 + 4) * lx));
+  if (!on1) return direct;
+  const R L = fmadd(P::ldw(phr), -cdt, lx);
+  if (OWN) P::st(phw, P::cfg(q.q1) * L);
+  return fmadd(direct, P::cfg(q.q1 + 3), L);
+}
+
+// Curl weight of the Hy point (i, j): lambda_D2, D2 = E(i+1, j) - E(i, j).
+template <class P, bool OWN>
+__device__ __forceinline__ typename P::R adj_y(const GridDev& g, int i, int j,
+                                               const typename P::T* lyp,
+                                               const typename P::T* phr, typename P::T* phw) {
+  using R = typename P::R;
+  const ClassCoef& cc = class_y(g, i, j);
+  const int kind = __ldg(&cc.kind);
+  if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return P::zero();
+  const R ly = P::ldw(lyp);
+  if (kind == GMES_KIND_DIELECTRIC) return P::cfg(&cc.c2) * ly;
+  const Prof q = prof_y(g, __ldg(&cc.pml), i, j);
+  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
+  if (!on1 && !on2) return P::cfg(&cc.c2) * ly;
+  const R cdt = P::cfg(&cc.cdt);
+  const R direct = cdt * (P::cfg(q.q2 + 4) * ly);
+  if (!on2) return direct;
+  const R L = fmadd(P::ldw(phr), cdt, ly);
+  if (OWN) P::st(phw, P::cfg(q.q2) * L);
+  return fmadd(direct, P::cfg(q.q2 + 3), L);
+}
+
+// Curl weights (lambda_D1, lambda_D2) of the Ez point (i, j) of design b
+// from its adjoint *lep; phr0/phr1: its two psi adjoints before this step,
+// OWN: the advanced ones are written to *phw0/*phw1.  NEED1/NEED2: which
+// weights the caller uses (both when OWN).
+template <class P, bool OWN, bool NEED1, bool NEED2>
+__device__ __forceinline__ void adj_e(const GridDev& g, const TmzDev& t, int b, int i, int j,
+                                      const typename P::T* lep, const typename P::T* phr0,
+                                      typename P::T* phw0, const typename P::T* phr1,
+                                      typename P::T* phw1, typename P::R& w1,
+                                      typename P::R& w2) {
+  using R = typename P::R;
+  w1 = P::zero();
+  w2 = P::zero();
+  const int64_t dp = design_index(t, i, j);
+  R c1, c2;
+  if (dp >= 0) {
+    const DesignCoef* dc = t.dc + (int64_t)b * t.dn[0] * t.dn[1] + dp;
+    c1 = P::cfg(&dc->c1);
+    c2 = P::cfg(&dc->c2);
+  } else {
+    const ClassCoef& cc = class_e(g, i, j);
+    const int kind = __ldg(&cc.kind);
+    if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return;
+    c1 = P::cfg(&cc.c1);
+    c2 = P::cfg(&cc.c2);
+    if (kind == GMES_KIND_CPML) {
+      const Prof q = prof_e(g, __ldg(&cc.pml), i, j);
+      const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
+      if (on1 || on2) {
+        const R le = P::ldw(lep);
+        const R cdt = P::cfg(&cc.cdt);
+        if (NEED1 || OWN) {
+          const R direct = cdt * (P::cfg(q.q1 + 4) * le);
+          if (on1) {
+            const R L = fmadd(P::ldw(phr0), cdt, le);
+            if (OWN) P::st(phw0, P::cfg(q.q1) * L);
+            w1 = fmadd(direct, P::cfg(q.q1 + 3), L);
+          } else {
+            w1 = direct;
+          }
+        }
+        if (NEED2 || OWN) {
+          const R direct = -(cdt * (P::cfg(q.q2 + 4) * le));
+          if (on2) {
+            const R L = fmadd(P::ldw(phr1), -cdt, le);
+            if (OWN) P::st(phw1, P::cfg(q.q2) * L);
+            w2 = fmadd(direct, P::cfg(q.q2 + 3), L);
+          } else {
+            w2 = direct;
+          }
+        }
+        return;
+      }
+    }
+  }
+  const R le = P::ldw(lep);
+  if (NEED1 || OWN) w1 = c1 * le;
+  if (NEED2 || OWN) w2 = -(c2 * le);
+}
+
+// Objective seed of lattice point (i, j) of design b at reverse step n:
+// dJ/dE_n = 2 dt w_b E_n on monitor points (*has), nothing elsewhere.
+__device__ __forceinline__ double seed_of(const GridDev& g, const TmzDev& t, int b, int i, int j,
+                                          int n, bool* has) {
+  const int64_t m = monitor_index(t, i, j);
+  *has = m >= 0;
+  if (m < 0) return 0.0;
+  const int64_t nm = (int64_t)t.mn[0] * t.mn[1];
+  const double w = t.weight != nullptr ? t.weight[b] : 1.0;
+  const double e = t.mon[((int64_t)b * t.total_steps + (n - 1)) * nm + m];
+  return 2.0 * g.dt * w * e;
+}
+
+// ---------------------------------------------------------------------------
+// The resolved lattice map.
+// ---------------------------------------------------------------------------
+// Whether a CPML point's profile is on along either curl axis.
+__device__ __forceinline__ bool profile_on(const Prof& q) {
+  return coef_nonzero(q.q1 + 1) || coef_nonzero(q.q2 + 1);
+}
+
+template <class P>
+__device__ __forceinline__ const typename P::T* map_coef(const TmzDev& t, int k) {
+  return static_cast<const typename P::T*>(t.pcoef[k]);
+}
+
+// Flags and plain-form coefficients of every lattice point, built once per
+// design set from the class maps, class table and CPML profiles.  The
+// coefficients are the values the per-point functions read (c1, c2 of a
+// Dielectric class, or of a CPML class outside both profiles), so the
+// plain form reproduces them bit for bit.  Design pixels take their
+// coefficients from the per-design table.
+template <class P>
+__global__ void k_tmz_map(const GridDev g, const TmzDev t) {
+  using R = typename P::R;
+  using T = typename P::T;
+  const int64_t ll = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ll >= t.plane) return;
+  const int i = (int)(ll / t.ny), j = (int)(ll - (int64_t)i * t.ny);
+  unsigned f = 0;
+  R c1 = P::zero(), c2n = P::zero(), cxn = P::zero(), cy = P::zero();
+  if (design_index(t, i, j) >= 0) {
+    f |= kTmzPlainE | kTmzDesign;
+  } else {
+    const ClassCoef& cc = class_e(g, i, j);
+    const int kind = __ldg(&cc.kind);
+    if (kind == GMES_KIND_CPML && profile_on(prof_e(g, __ldg(&cc.pml), i, j))) {
+      f |= kTmzPsiE;
+    } else if (kind == GMES_KIND_DIELECTRIC || kind == GMES_KIND_CPML) {
+      f |= kTmzPlainE;
+      c1 = P::cfg(&cc.c1);
+      c2n = -P::cfg(&cc.c2);
+    }
+  }
+  {
+    const ClassCoef& cc = class_x(g, i, j);
+    const int kind = __ldg(&cc.kind);
+    if (kind == GMES_KIND_CPML && profile_on(prof_x(g, __ldg(&cc.pml), i, j))) {
+      f |= kTmzPsiX;
+    } else if (kind == GMES_KIND_DIELECTRIC || kind == GMES_KIND_CPML) {
+      f |= kTmzPlainX;
+      cxn = -P::cfg(&cc.c1);
+    }
+  }
+  {
+    const ClassCoef& cc = class_y(g, i, j);
+    const int kind = __ldg(&cc.kind);
+    if (kind == GMES_KIND_CPML && profile_on(prof_y(g, __ldg(&cc.pml), i, j))) {
+      f |= kTmzPsiY;
+    } else if (kind == GMES_KIND_DIELECTRIC || kind == GMES_KIND_CPML) {
+      f |= kTmzPlainY;
+      cy = P::cfg(&cc.c2);
+    }
+  }
+  if (monitor_index(t, i, j) >= 0) f |= kTmzMonitor;
+  const_cast<uint32_t*>(t.pflags)[ll] = f;
+  P::st(const_cast<T*>(map_coef<P>(t, 0)) + ll, c1);
+  P::st(const_cast<T*>(map_coef<P>(t, 1)) + ll, c2n);
+  P::st(const_cast<T*>(map_coef<P>(t, 2)) + ll, cxn);
+  P::st(const_cast<T*>(map_coef<P>(t, 3)) + ll, cy);
+}
+
+// Marks the points that carry a point source of either half (after
+// k_tmz_map, which clears those bits).
+__global__ void k_tmz_map_sources(const TmzDev t) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= t.nsrc) return;
+  const gmes_point_source s = t.src[k];
+  if (s.comp < 2 || s.comp > 4 || s.offset < 0 || s.offset >= t.plane) return;
+  atomicOr(const_cast<uint32_t*>(t.pflags) + s.offset, s.comp == 2 ? kTmzSrcE : kTmzSrcH);
+}
+
+// Plain-form Ez coefficients (c1, -c2) of lattice point (i, j) = ll of
+// design b.
+template <class P>
+__device__ __forceinline__ void e_coef(const TmzDev& t, int b, int i, int j, int64_t ll,
+                                       unsigned fl, typename P::R& c1, typename P::R& c2n) {
+  c1 = P::ld(map_coef<P>(t, 0) + ll);
+  c2n = P::ld(map_coef<P>(t, 1) + ll);
+  if (fl & kTmzDesign) {
+    const DesignCoef* dc = t.dc + (int64_t)b * t.dn[0] * t.dn[1] + design_index(t, i, j);
+    c1 = P::cfg(&dc->c1);
+    c2n = -P::cfg(&dc->c2);
+  }
+}
+
+// Adjoint curl weights through the map: the plain form, or the per-point
+// functions on CPML points inside a profile.  ll: lattice offset; base:
+// the design's offset.
+template <class P, bool OWN>
+__device__ __forceinline__ typename P::R weight_x(const GridDev& g, const TmzDev& t, int i, int j,
+                                                  int64_t ll, int64_t base, int rb, int wb) {
+  using T = typename P::T;
+  const T* lx = static_cast<const T*>(t.l[1]) + base + ll;
+  const typename P::R c = P::ld(map_coef<P>(t, 2) + ll);  // issued with the flags
+  if (__ldg(t.pflags + ll) & kTmzPlainX) return c * P::ldw(lx);
+  return adj_x<P, OWN>(g, i, j, lx, static_cast<const T*>(t.phi[rb][2]) + base + ll,
+                       OWN ? static_cast<T*>(t.phi[wb][2]) + base + ll : nullptr);
+}
+
+template <class P, bool OWN>
+__device__ __forceinline__ typename P::R weight_y(const GridDev& g, const TmzDev& t, int i, int j,
+                                                  int64_t ll, int64_t base, int rb, int wb) {
+  using T = typename P::T;
+  const T* ly = static_cast<const T*>(t.l[2]) + base + ll;
+  const typename P::R c = P::ld(map_coef<P>(t, 3) + ll);  // issued with the flags
+  if (__ldg(t.pflags + ll) & kTmzPlainY) return c * P::ldw(ly);
+  return adj_y<P, OWN>(g, i, j, ly, static_cast<const T*>(t.phi[rb][3]) + base + ll,
+                       OWN ? static_cast<T*>(t.phi[wb][3]) + base + ll : nullptr);
+}
+
+template <class P, bool OWN, bool NEED1, bool NEED2>
+__device__ __forceinline__ void weight_e(const GridDev& g, const TmzDev& t, int b, int i, int j,
+                                         int64_t ll, int64_t base, int rb, int wb,
+                                         typename P::R& w1, typename P::R& w2) {
+  using R = typename P::R;
+  using T = typename P::T;
+  const T* le = static_cast<const T*>(t.l[0]) + base + ll;
+  const unsigned fl = __ldg(t.pflags + ll);
+  if (fl & kTmzPlainE) {
+    R c1, c2n;
+    e_coef<P>(t, b, i, j, ll, fl, c1, c2n);
+    const R v = P::ldw(le);
+    w1 = c1 * v;
+    w2 = c2n * v;
+    return;
+  }
+  adj_e<P, OWN, NEED1, NEED2>(g, t, b, i, j, le, static_cast<const T*>(t.phi[rb][0]) + base + ll,
+                              OWN ? static_cast<T*>(t.phi[wb][0]) + base + ll : nullptr,
+                              static_cast<const T*>(t.phi[rb][1]) + base + ll,
+                              OWN ? static_cast<T*>(t.phi[wb][1]) + base + ll : nullptr, w1, w2);
+}
+
+// ---------------------------------------------------------------------------
+// One-step forward kernels.
 // ---------------------------------------------------------------------------
 template <class P>
 __global__ void __launch_bounds__(kBX* kBY) k_tmz_fe(const GridDev g, const TmzDev t, int slot) {
@@ -110,43 +491,26 @@ __global__ void __launch_bounds__(kBX* kBY) k_tmz_fe(const GridDev g, const TmzD
   T* E = static_cast<T*>(t.f[0]) + p.base;
   const T* X = static_cast<const T*>(t.f[1]) + p.base;
   const T* Y = static_cast<const T*>(t.f[2]) + p.base;
-  const R e = P::ldw(E + p.lin);
+  const unsigned fl = __ldg(t.pflags + p.lin);
   const R D1 = P::ld(Y + p.lin) - P::ld(Y + (int64_t)im * t.ny + p.j);
   const R D2 = P::ld(X + p.lin) - P::ld(X + (int64_t)p.i * t.ny + jm);
-  const int64_t dp = design_index(t, p.i, p.j);
-  if (dp >= 0) {
-    const int64_t nd = (int64_t)t.dn[0] * t.dn[1];
-    const DesignCoef* dc = t.dc + (int64_t)p.b * nd + dp;
-    const R c1 = P::cfg(&dc->c1), c2 = P::cfg(&dc->c2);
-    P::st(E + p.lin, (e + c1 * D1) - c2 * D2);
-    if (slot >= 0)
-      P::st(static_cast<T*>(t.hist) + ((int64_t)slot * t.nb + p.b) * nd + dp, c1 * D1 - c2 * D2);
-    return;
-  }
-  const ClassCoef& cc = class_e(g, p.i, p.j);
-  const int kind = __ldg(&cc.kind);
-  if (kind == GMES_KIND_DIELECTRIC) {
-    P::st(E + p.lin, (e + P::cfg(&cc.c1) * D1) - P::cfg(&cc.c2) * D2);
-  } else if (kind == GMES_KIND_CPML) {
-    const Prof q = prof_e(g, __ldg(&cc.pml), p.i, p.j);
-    const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-    if (!on1 && !on2) {
-      P::st(E + p.lin, (e + P::cfg(&cc.c1) * D1) - P::cfg(&cc.c2) * D2);
-      return;
+  const R e = P::ldw(E + p.lin);
+  if (fl & kTmzPlainE) {
+    R c1, c2n;
+    e_coef<P>(t, p.b, p.i, p.j, p.lin, fl, c1, c2n);
+    P::st(E + p.lin, fmadd(fmadd(e, c1, D1), c2n, D2));
+    if ((fl & kTmzDesign) && slot >= 0) {
+      const int64_t nd = (int64_t)t.dn[0] * t.dn[1];
+      P::st(static_cast<T*>(t.hist) + ((int64_t)slot * t.nb + p.b) * nd +
+                design_index(t, p.i, p.j),
+            fmadd(c2n * D2, c1, D1));
     }
-    T* s1 = static_cast<T*>(t.f[3]) + p.base + p.lin;
-    T* s2 = static_cast<T*>(t.f[4]) + p.base + p.lin;
-    R psi1 = P::ldw(s1), psi2 = P::ldw(s2);
-    if (on1) {
-      psi1 = P::cfg(q.q1) * psi1 + P::cfg(q.q1 + 3) * D1;
-      P::st(s1, psi1);
-    }
-    if (on2) {
-      psi2 = P::cfg(q.q2) * psi2 + P::cfg(q.q2 + 3) * D2;
-      P::st(s2, psi2);
-    }
-    const R xv = ((psi1 - psi2) + P::cfg(q.q1 + 4) * D1) - P::cfg(q.q2 + 4) * D2;
-    P::st(E + p.lin, e + P::cfg(&cc.cdt) * xv);
+  } else if (fl & kTmzPsiE) {
+    int64_t dp;
+    R inc;
+    P::st(E + p.lin, e_point<P>(g, t, p.b, p.i, p.j, e, D1, D2,
+                                static_cast<T*>(t.f[3]) + p.base + p.lin,
+                                static_cast<T*>(t.f[4]) + p.base + p.lin, &dp, &inc));
   }
 }
 
@@ -160,59 +524,24 @@ __global__ void __launch_bounds__(kBX* kBY) k_tmz_fh(const GridDev g, const TmzD
   const T* E = static_cast<const T*>(t.f[0]) + p.base;
   T* X = static_cast<T*>(t.f[1]) + p.base;
   T* Y = static_cast<T*>(t.f[2]) + p.base;
+  const unsigned fl = __ldg(t.pflags + p.lin);
+  const R cxn = P::ld(map_coef<P>(t, 2) + p.lin), cy = P::ld(map_coef<P>(t, 3) + p.lin);
   const R e0 = P::ld(E + p.lin);
   const R dx = P::ld(E + (int64_t)p.i * t.ny + jp) - e0;  // D1 of Hx
   const R dy = P::ld(E + (int64_t)ip * t.ny + p.j) - e0;  // D2 of Hy
-  {
-    const ClassCoef& cc = class_x(g, p.i, p.j);
-    const int kind = __ldg(&cc.kind);
-    const R x = P::ldw(X + p.lin);
-    if (kind == GMES_KIND_DIELECTRIC) {
-      P::st(X + p.lin, x - P::cfg(&cc.c1) * dx);
-    } else if (kind == GMES_KIND_CPML) {
-      const Prof q = prof_x(g, __ldg(&cc.pml), p.i, p.j);
-      const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-      if (!on1 && !on2) {
-        P::st(X + p.lin, x - P::cfg(&cc.c1) * dx);
-      } else {
-        T* s = static_cast<T*>(t.f[5]) + p.base + p.lin;
-        R psi = P::ldw(s);
-        if (on1) {
-          psi = P::cfg(q.q1) * psi + P::cfg(q.q1 + 3) * dx;
-          P::st(s, psi);
-        }
-        P::st(X + p.lin, x - P::cfg(&cc.cdt) * (psi + P::cfg(q.q1 + 4) * dx));
-      }
-    }
-  }
-  {
-    const ClassCoef& cc = class_y(g, p.i, p.j);
-    const int kind = __ldg(&cc.kind);
-    const R y = P::ldw(Y + p.lin);
-    if (kind == GMES_KIND_DIELECTRIC) {
-      P::st(Y + p.lin, y + P::cfg(&cc.c2) * dy);
-    } else if (kind == GMES_KIND_CPML) {
-      const Prof q = prof_y(g, __ldg(&cc.pml), p.i, p.j);
-      const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-      if (!on1 && !on2) {
-        P::st(Y + p.lin, y + P::cfg(&cc.c2) * dy);
-      } else {
-        T* s = static_cast<T*>(t.f[6]) + p.base + p.lin;
-        R psi = P::ldw(s);
-        if (on2) {
-          psi = P::cfg(q.q2) * psi + P::cfg(q.q2 + 3) * dy;
-          P::st(s, psi);
-        }
-        P::st(Y + p.lin, y - P::cfg(&cc.cdt) * ((-psi) - P::cfg(q.q2 + 4) * dy));
-      }
-    }
-  }
-  if (row >= 0) {
-    const int64_t m = monitor_index(t, p.i, p.j);
-    if (m >= 0) {
-      const int64_t nm = (int64_t)t.mn[0] * t.mn[1];
-      t.mon[((int64_t)p.b * t.total_steps + row) * nm + m] = to_double(e0);
-    }
+  if (fl & kTmzPlainX)
+    P::st(X + p.lin, fmadd(P::ldw(X + p.lin), cxn, dx));
+  else if (fl & kTmzPsiX)
+    P::st(X + p.lin, x_point<P>(g, p.i, p.j, P::ldw(X + p.lin), dx,
+                                static_cast<T*>(t.f[5]) + p.base + p.lin));
+  if (fl & kTmzPlainY)
+    P::st(Y + p.lin, fmadd(P::ldw(Y + p.lin), cy, dy));
+  else if (fl & kTmzPsiY)
+    P::st(Y + p.lin, y_point<P>(g, p.i, p.j, P::ldw(Y + p.lin), dy,
+                                static_cast<T*>(t.f[6]) + p.base + p.lin));
+  if (row >= 0 && (fl & kTmzMonitor)) {
+    const int64_t nm = (int64_t)t.mn[0] * t.mn[1];
+    t.mon[((int64_t)p.b * t.total_steps + row) * nm + monitor_index(t, p.i, p.j)] = to_double(e0);
   }
 }
 
@@ -237,112 +566,8 @@ __global__ void k_tmz_src(const TmzDev t, int side, int n) {
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint.
+// One-step adjoint kernels.
 // ---------------------------------------------------------------------------
-// Curl weight of the Hx point (i, j): lambda_D1 = dX'/dD1 applied to
-// lambda_X, with D1 = E(i, j+1) - E(i, j).  OWN: also write the psi adjoint.
-template <class P, bool OWN>
-__device__ __forceinline__ typename P::R adj_x(const GridDev& g, const TmzDev& t, int64_t base,
-                                               int i, int j, int rb, int wb) {
-  using R = typename P::R;
-  using T = typename P::T;
-  const int64_t lin = (int64_t)i * t.ny + j;
-  const ClassCoef& cc = class_x(g, i, j);
-  const int kind = __ldg(&cc.kind);
-  if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return P::zero();
-  const R lx = P::ldw(static_cast<const T*>(t.l[1]) + base + lin);
-  if (kind == GMES_KIND_DIELECTRIC) return -(P::cfg(&cc.c1) * lx);
-  const Prof q = prof_x(g, __ldg(&cc.pml), i, j);
-  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-  if (!on1 && !on2) return -(P::cfg(&cc.c1) * lx);
-  const R cdt = P::cfg(&cc.cdt);
-  const R direct = -(cdt * (P::cfg(q.q1 + 4) * lx));
-  if (!on1) return direct;
-  const R L = P::ldw(static_cast<const T*>(t.phi[rb][2]) + base + lin) - cdt * lx;
-  if (OWN) P::st(static_cast<T*>(t.phi[wb][2]) + base + lin, P::cfg(q.q1) * L);
-  return P::cfg(q.q1 + 3) * L + direct;
-}
-
-// Curl weight of the Hy point (i, j): lambda_D2, D2 = E(i+1, j) - E(i, j).
-template <class P, bool OWN>
-__device__ __forceinline__ typename P::R adj_y(const GridDev& g, const TmzDev& t, int64_t base,
-                                               int i, int j, int rb, int wb) {
-  using R = typename P::R;
-  using T = typename P::T;
-  const int64_t lin = (int64_t)i * t.ny + j;
-  const ClassCoef& cc = class_y(g, i, j);
-  const int kind = __ldg(&cc.kind);
-  if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return P::zero();
-  const R ly = P::ldw(static_cast<const T*>(t.l[2]) + base + lin);
-  if (kind == GMES_KIND_DIELECTRIC) return P::cfg(&cc.c2) * ly;
-  const Prof q = prof_y(g, __ldg(&cc.pml), i, j);
-  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-  if (!on1 && !on2) return P::cfg(&cc.c2) * ly;
-  const R cdt = P::cfg(&cc.cdt);
-  const R direct = cdt * (P::cfg(q.q2 + 4) * ly);
-  if (!on2) return direct;
-  const R L = P::ldw(static_cast<const T*>(t.phi[rb][3]) + base + lin) + cdt * ly;
-  if (OWN) P::st(static_cast<T*>(t.phi[wb][3]) + base + lin, P::cfg(q.q2) * L);
-  return P::cfg(q.q2 + 3) * L + direct;
-}
-
-// Curl weights (lambda_D1, lambda_D2) of the Ez point (i, j) of design b.
-template <class P, bool OWN, bool NEED1, bool NEED2>
-__device__ __forceinline__ void adj_e(const GridDev& g, const TmzDev& t, int b, int64_t base,
-                                      int i, int j, int rb, int wb, typename P::R& w1,
-                                      typename P::R& w2) {
-  using R = typename P::R;
-  using T = typename P::T;
-  const int64_t lin = (int64_t)i * t.ny + j;
-  w1 = P::zero();
-  w2 = P::zero();
-  const int64_t dp = design_index(t, i, j);
-  R c1, c2;
-  if (dp >= 0) {
-    const DesignCoef* dc = t.dc + (int64_t)b * t.dn[0] * t.dn[1] + dp;
-    c1 = P::cfg(&dc->c1);
-    c2 = P::cfg(&dc->c2);
-  } else {
-    const ClassCoef& cc = class_e(g, i, j);
-    const int kind = __ldg(&cc.kind);
-    if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return;
-    c1 = P::cfg(&cc.c1);
-    c2 = P::cfg(&cc.c2);
-    if (kind == GMES_KIND_CPML) {
-      const Prof q = prof_e(g, __ldg(&cc.pml), i, j);
-      const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-      if (on1 || on2) {
-        const R le = P::ldw(static_cast<const T*>(t.l[0]) + base + lin);
-        const R cdt = P::cfg(&cc.cdt);
-        if (NEED1 || OWN) {
-          const R direct = cdt * (P::cfg(q.q1 + 4) * le);
-          if (on1) {
-            const R L = P::ldw(static_cast<const T*>(t.phi[rb][0]) + base + lin) + cdt * le;
-            if (OWN) P::st(static_cast<T*>(t.phi[wb][0]) + base + lin, P::cfg(q.q1) * L);
-            w1 = P::cfg(q.q1 + 3) * L + direct;
-          } else {
-            w1 = direct;
-          }
-        }
-        if (NEED2 || OWN) {
-          const R direct = -(cdt * (P::cfg(q.q2 + 4) * le));
-          if (on2) {
-            const R L = P::ldw(static_cast<const T*>(t.phi[rb][1]) + base + lin) - cdt * le;
-            if (OWN) P::st(static_cast<T*>(t.phi[wb][1]) + base + lin, P::cfg(q.q2) * L);
-            w2 = P::cfg(q.q2 + 3) * L + direct;
-          } else {
-            w2 = direct;
-          }
-        }
-        return;
-      }
-    }
-  }
-  const R le = P::ldw(static_cast<const T*>(t.l[0]) + base + lin);
-  if (NEED1 || OWN) w1 = c1 * le;
-  if (NEED2 || OWN) w2 = -(c2 * le);
-}
-
 // Transpose of the H half of step n, plus the objective's seed for the
 // state after step n: lambda_E gathers the curl weights of its four H
 // neighbours; the owner advances the Hx/Hy psi adjoints.
@@ -356,17 +581,15 @@ __global__ void __launch_bounds__(kBX* kBY)
   const int im = p.i == 0 ? t.nx - 1 : p.i - 1, jm = p.j == 0 ? t.ny - 1 : p.j - 1;
   T* LE = static_cast<T*>(t.l[0]) + p.base + p.lin;
   R le = P::ldw(LE);
-  const int64_t m = monitor_index(t, p.i, p.j);
-  if (m >= 0) {
-    const int64_t nm = (int64_t)t.mn[0] * t.mn[1];
-    const double w = t.weight != nullptr ? t.weight[p.b] : 1.0;
-    const double e = t.mon[((int64_t)p.b * t.total_steps + (n - 1)) * nm + m];
-    le = le + P::from_double(2.0 * g.dt * w * e);
+  if (__ldg(t.pflags + p.lin) & kTmzMonitor) {
+    bool has;
+    le = le + P::from_double(seed_of(g, t, p.b, p.i, p.j, n, &has));
   }
-  const R a = adj_x<P, false>(g, t, p.base, p.i, jm, rb, wb);
-  const R bx = adj_x<P, true>(g, t, p.base, p.i, p.j, rb, wb);
-  const R c = adj_y<P, false>(g, t, p.base, im, p.j, rb, wb);
-  const R d = adj_y<P, true>(g, t, p.base, p.i, p.j, rb, wb);
+  const int64_t ljm = (int64_t)p.i * t.ny + jm, lim = (int64_t)im * t.ny + p.j;
+  const R a = weight_x<P, false>(g, t, p.i, jm, ljm, p.base, rb, wb);
+  const R bx = weight_x<P, true>(g, t, p.i, p.j, p.lin, p.base, rb, wb);
+  const R c = weight_y<P, false>(g, t, im, p.j, lim, p.base, rb, wb);
+  const R d = weight_y<P, true>(g, t, p.i, p.j, p.lin, p.base, rb, wb);
   P::st(LE, le + ((a - bx) + (c - d)));
 }
 
@@ -381,17 +604,18 @@ __global__ void __launch_bounds__(kBX* kBY)
   Lat p;
   if (!lattice_point(t, p)) return;
   const int ip = p.i + 1 == t.nx ? 0 : p.i + 1, jp = p.j + 1 == t.ny ? 0 : p.j + 1;
+  const int64_t ljp = (int64_t)p.i * t.ny + jp, lip = (int64_t)ip * t.ny + p.j;
   R w1, w2, u1, u2, v1, v2;
-  adj_e<P, true, true, true>(g, t, p.b, p.base, p.i, p.j, rb, wb, w1, w2);
-  adj_e<P, false, false, true>(g, t, p.b, p.base, p.i, jp, rb, wb, u1, u2);
-  adj_e<P, false, true, false>(g, t, p.b, p.base, ip, p.j, rb, wb, v1, v2);
+  weight_e<P, true, true, true>(g, t, p.b, p.i, p.j, p.lin, p.base, rb, wb, w1, w2);
+  weight_e<P, false, false, true>(g, t, p.b, p.i, jp, ljp, p.base, rb, wb, u1, u2);
+  weight_e<P, false, true, false>(g, t, p.b, ip, p.j, lip, p.base, rb, wb, v1, v2);
   T* LX = static_cast<T*>(t.l[1]) + p.base + p.lin;
   T* LY = static_cast<T*>(t.l[2]) + p.base + p.lin;
   P::st(LX, P::ldw(LX) + (w2 - u2));
   P::st(LY, P::ldw(LY) + (w1 - v1));
-  const int64_t dp = design_index(t, p.i, p.j);
-  if (dp >= 0) {
+  if (__ldg(t.pflags + p.lin) & kTmzDesign) {
     const int64_t nd = (int64_t)t.dn[0] * t.dn[1];
+    const int64_t dp = design_index(t, p.i, p.j);
     const int64_t k = (int64_t)p.b * nd + dp;
     const double le = to_double(P::ldw(static_cast<const T*>(t.l[0]) + p.base + p.lin));
     const double inc =
@@ -413,6 +637,368 @@ __global__ void k_tmz_adj_src(const TmzDev t, int side) {
   if (s.offset < 0 || s.offset >= t.plane) return;
   P::st(static_cast<typename P::T*>(t.l[s.comp - 2]) + (int64_t)b * t.plane + s.offset,
         P::zero());
+}
+
+// ---------------------------------------------------------------------------
+// Temporally blocked kernels (FP32).
+// ---------------------------------------------------------------------------
+// A block owns a TI x TJ tile of one design's lattice and keeps the region
+// of RI x RJ = (TI + 2 H) x (TJ + 2 H) points around it in shared memory
+// (region point (a, c) is lattice point (ri0 + a, rj0 + c) taken periodically,
+// so tiles at the lattice edge see its periodic images).  An E update reads
+// its low-side neighbours (i-1, j-1) and an H update its high-side ones
+// (i+1, j+1); updating every region point that has its neighbours in the
+// region, each half-step leaves the values exact on the region shrunk by
+// one more row and column on one side.  After s <= H steps the values are
+// exact on [s, RI-1-s] (H fields) and [s, RI-s] (E), which contain the tile,
+// so the tile is written back and the next launch reloads fresh halos.
+// DRAM traffic per step falls from a read and write of every field per
+// half-step to one read of the region and one write of the tile per H
+// steps.  Sources, monitors, design increments and gradients are applied
+// as in the one-step kernels: sources to every copy of their point in the
+// region, records and gradients only from tile points.
+//
+// Each launch reads every region point's flags and plain-form
+// coefficients from the resolved map once and keeps them in registers, so
+// a sub-step of a plain point is a few shared-memory operations; CPML
+// points inside a profile go through the per-point functions above.
+//
+// Threads: RJ = 64 columns x 8 rows; a thread owns column c of rows
+// ty, ty + 8, ...; psi (and psi adjoint) values are loaded and stored only
+// on CPML points inside a profile.
+constexpr int kTbHalo = GMES_TMZ_MAX_BLOCK_STEPS;  // most steps per launch
+constexpr int kTbRJ = 64;    // region columns (j)
+constexpr int kTbRows = 8;   // thread rows
+constexpr int kTbThreads = kTbRJ * kTbRows;
+constexpr int kTbRI = 32;    // region rows (i)
+#ifndef GMES_TB_MIN_BLOCKS
+#define GMES_TB_MIN_BLOCKS 2
+#endif
+constexpr int kTbMinBlocks = GMES_TB_MIN_BLOCKS;  // resident blocks per SM (register budget)
+
+__device__ __forceinline__ int wrap_index(int v, int n) {
+  if (v < 0) v += n;
+  if (v >= n) v -= n;
+  if (v >= 0 && v < n) return v;
+  v %= n;  // regions wider than twice the lattice
+  return v < 0 ? v + n : v;
+}
+
+template <int RI>
+struct TbGeom {
+  static constexpr int H = kTbHalo, RJ = kTbRJ, TI = RI - 2 * kTbHalo, TJ = kTbRJ - 2 * kTbHalo;
+  static constexpr int NP = RI * kTbRJ, Q = RI / kTbRows;
+  static_assert(RI % kTbRows == 0 && TI > 0, "region rows");
+};
+
+// Plain-form coefficients of one region point.
+struct TbPoint {
+  float c1, c2n;  // Ez: c1, -c2
+  float cxn, cy;  // Hx: -c1, Hy: c2
+};
+
+// Flags and plain-form coefficients of lattice point (i, j) of design b,
+// from the resolved map.
+__device__ __forceinline__ unsigned tb_point(const TmzDev& t, int b, int i, int j, TbPoint& p) {
+  using P = PolF32;
+  const int64_t ll = (int64_t)i * t.ny + j;
+  const unsigned f = __ldg(t.pflags + ll);
+  e_coef<P>(t, b, i, j, ll, f, p.c1, p.c2n);
+  p.cxn = __ldg(map_coef<P>(t, 2) + ll);
+  p.cy = __ldg(map_coef<P>(t, 3) + ll);
+  return f;
+}
+
+// Apply this half's sources of step n to every copy of their point in the
+// region: the forward (ADJ false: hard sources set the value, current
+// sources subtract theirs) or the adjoint (ADJ true: hard sources zero it).
+template <bool ADJ>
+__device__ __forceinline__ void tb_sources(const TmzDev& t, int side, int n, int ri0, int rj0,
+                                           int RI, int RJ, float* fE, float* fX, float* fY) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  for (int k = tid; k < t.nsrc; k += kTbThreads) {
+    const gmes_point_source s = t.src[k];
+    if (s.comp < 2 || s.comp > 4 || (s.comp == 2) != (side == 0)) continue;
+    if (s.offset < 0 || s.offset >= t.plane) continue;
+    if (ADJ && s.mode != 0) continue;
+    const int li = (int)(s.offset / t.ny), lj = (int)(s.offset - (int64_t)li * t.ny);
+    float* f = s.comp == 2 ? fE : (s.comp == 3 ? fX : fY);
+    const float v =
+        ADJ ? 0.f
+            : PolF32::from_double(t.src_val[((int64_t)(n - 1) * 2 + side) * t.nsrc + k]);
+    for (int a = wrap_index(li - ri0, t.nx); a < RI; a += t.nx)
+      for (int c = wrap_index(lj - rj0, t.ny); c < RJ; c += t.ny) {
+        float* q = f + a * RJ + c;
+        *q = (ADJ || s.mode == 0) ? v : *q - v;
+      }
+  }
+}
+
+// Forward steps n0+1 .. n0+nsub (nsub <= kTbHalo) of one tile, from the
+// state in t.f to the state in t.tmp (the launch's other blocks still read
+// t.f for their halos, so the result must not overwrite it).  slot0 >= 0:
+// record the design increments of step n0+1+s at hist slot slot0+s;
+// rec_mon: record monitor row n-1 of every step n.
+template <int RI>
+__global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
+    k_tmz_tb_fwd(const GridDev g, const TmzDev t, int n0, int nsub, int slot0, int rec_mon) {
+  using P = PolF32;
+  using G = TbGeom<RI>;
+  constexpr int H = G::H, RJ = G::RJ, TI = G::TI, TJ = G::TJ, NP = G::NP, Q = G::Q;
+  extern __shared__ float4 tb_smem[];
+  float* sE = reinterpret_cast<float*>(tb_smem);
+  float* sX = sE + NP;
+  float* sY = sX + NP;
+  float* sS = sY + NP;  // psi of Ez (x, y), Hx, Hy: sS + k * NP
+  const int c = threadIdx.x, ty = threadIdx.y, b = blockIdx.z;
+  const int ri0 = (int)blockIdx.y * TI - H, rj0 = (int)blockIdx.x * TJ - H;
+  const int j = wrap_index(rj0 + c, t.ny);
+  const bool jtile = c >= H && c < H + TJ && rj0 + c < t.ny;
+  const int64_t base = (int64_t)b * t.plane;
+  int li[Q];
+  TbPoint pt[Q];
+  unsigned fl[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int a = ty + kTbRows * q, k = a * RJ + c;
+    li[q] = wrap_index(ri0 + a, t.nx);
+    fl[q] = tb_point(t, b, li[q], j, pt[q]);
+    if (jtile && a >= H && a < H + TI && ri0 + a < t.nx) fl[q] |= 1u << 31;  // tile point
+    const int64_t lin = base + (int64_t)li[q] * t.ny + j;
+    sE[k] = __ldg(static_cast<const float*>(t.f[0]) + lin);
+    sX[k] = __ldg(static_cast<const float*>(t.f[1]) + lin);
+    sY[k] = __ldg(static_cast<const float*>(t.f[2]) + lin);
+    if (fl[q] & kTmzPsiE) {
+      sS[k] = __ldg(static_cast<const float*>(t.f[3]) + lin);
+      sS[NP + k] = __ldg(static_cast<const float*>(t.f[4]) + lin);
+    }
+    if (fl[q] & kTmzPsiX) sS[2 * NP + k] = __ldg(static_cast<const float*>(t.f[5]) + lin);
+    if (fl[q] & kTmzPsiY) sS[3 * NP + k] = __ldg(static_cast<const float*>(t.f[6]) + lin);
+  }
+  unsigned any = 0;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) any |= fl[q];
+  const bool src_e = __syncthreads_or(any & kTmzSrcE) != 0;  // also orders the loads
+  const bool src_h = __syncthreads_or(any & kTmzSrcH) != 0;
+  const int64_t nd = (int64_t)t.dn[0] * t.dn[1];
+  const int64_t nm = (int64_t)t.mn[0] * t.mn[1];
+  for (int s = 0; s < nsub; ++s) {
+    const int n = n0 + s + 1;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int a = ty + kTbRows * q, k = a * RJ + c;
+      if (a >= 1 && c >= 1) {
+        const float D1 = sY[k] - sY[k - RJ], D2 = sX[k] - sX[k - 1];
+        if (fl[q] & kTmzPlainE) {
+          sE[k] = fmadd(fmadd(sE[k], pt[q].c1, D1), pt[q].c2n, D2);
+          if ((fl[q] & kTmzDesign) && (fl[q] >> 31) && slot0 >= 0)
+            static_cast<float*>(t.hist)[((int64_t)(slot0 + s) * t.nb + b) * nd +
+                                        design_index(t, li[q], j)] =
+                fmadd(pt[q].c2n * D2, pt[q].c1, D1);
+        } else if (fl[q] & kTmzPsiE) {
+          int64_t dp;
+          float inc;
+          sE[k] = e_point<P>(g, t, b, li[q], j, sE[k], D1, D2, sS + k, sS + NP + k, &dp, &inc);
+        }
+      }
+    }
+    __syncthreads();
+    if (src_e) {
+      tb_sources<false>(t, 0, n, ri0, rj0, RI, RJ, sE, sX, sY);
+      __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int a = ty + kTbRows * q, k = a * RJ + c;
+      if (a < RI - 1 && c < RJ - 1) {
+        const float e0 = sE[k];
+        const float dx = sE[k + 1] - e0, dy = sE[k + RJ] - e0;
+        if (fl[q] & kTmzPlainX)
+          sX[k] = fmadd(sX[k], pt[q].cxn, dx);
+        else if (fl[q] & kTmzPsiX)
+          sX[k] = x_point<P>(g, li[q], j, sX[k], dx, sS + 2 * NP + k);
+        if (fl[q] & kTmzPlainY)
+          sY[k] = fmadd(sY[k], pt[q].cy, dy);
+        else if (fl[q] & kTmzPsiY)
+          sY[k] = y_point<P>(g, li[q], j, sY[k], dy, sS + 3 * NP + k);
+        if (rec_mon && (fl[q] & kTmzMonitor) && (fl[q] >> 31))
+          t.mon[((int64_t)b * t.total_steps + (n - 1)) * nm + monitor_index(t, li[q], j)] =
+              (double)e0;
+      }
+    }
+    __syncthreads();
+    if (src_h) {
+      tb_sources<false>(t, 1, n, ri0, rj0, RI, RJ, sE, sX, sY);
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    if (!(fl[q] >> 31)) continue;
+    const int k = (ty + kTbRows * q) * RJ + c;
+    const int64_t lin = base + (int64_t)li[q] * t.ny + j;
+    static_cast<float*>(t.tmp[0])[lin] = sE[k];
+    static_cast<float*>(t.tmp[1])[lin] = sX[k];
+    static_cast<float*>(t.tmp[2])[lin] = sY[k];
+    if (fl[q] & kTmzPsiE) {
+      static_cast<float*>(t.tmp[3])[lin] = sS[k];
+      static_cast<float*>(t.tmp[4])[lin] = sS[NP + k];
+    }
+    if (fl[q] & kTmzPsiX) static_cast<float*>(t.tmp[5])[lin] = sS[2 * NP + k];
+    if (fl[q] & kTmzPsiY) static_cast<float*>(t.tmp[6])[lin] = sS[3 * NP + k];
+  }
+}
+
+// Adjoint steps n0 + nsub down to n0 + 1 of one tile (the transposes of
+// k_tmz_ah / k_tmz_ae, same order), the field adjoints from t.l to
+// t.tmp[0..2]; the gradient of step n uses hist slot n - step0 - 1.  The
+// psi adjoints are read from the buffer step n0 + nsub reads
+// ((n0 + nsub) & 1) and written to the one step n0 + 1 writes, as the
+// one-step kernels do; nsub is odd, so the two buffers differ and no block
+// overwrites what another still reads.
+template <int RI>
+__global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
+    k_tmz_tb_adj(const GridDev g, const TmzDev t, int n0, int nsub, int step0) {
+  using P = PolF32;
+  using G = TbGeom<RI>;
+  constexpr int H = G::H, RJ = G::RJ, TI = G::TI, TJ = G::TJ, NP = G::NP, Q = G::Q;
+  extern __shared__ float4 tb_smem[];
+  float* sLE = reinterpret_cast<float*>(tb_smem);
+  float* sLX = sLE + NP;
+  float* sLY = sLX + NP;
+  float* sP = sLY + NP;      // psi adjoints of Ez (x, y), Hx, Hy: sP + k * NP
+  float* sW1 = sP + 4 * NP;  // curl weights: Hx, then Ez's first
+  float* sW2 = sW1 + NP;     // curl weights: Hy, then Ez's second
+  const int c = threadIdx.x, ty = threadIdx.y, b = blockIdx.z;
+  const int ri0 = (int)blockIdx.y * TI - H, rj0 = (int)blockIdx.x * TJ - H;
+  const int j = wrap_index(rj0 + c, t.ny);
+  const bool jtile = c >= H && c < H + TJ && rj0 + c < t.ny;
+  const int64_t base = (int64_t)b * t.plane;
+  const int rb = (n0 + nsub) & 1, wb = ((n0 + 1) & 1) ^ 1;
+  int li[Q];
+  TbPoint pt[Q];
+  unsigned fl[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int a = ty + kTbRows * q, k = a * RJ + c;
+    li[q] = wrap_index(ri0 + a, t.nx);
+    fl[q] = tb_point(t, b, li[q], j, pt[q]);
+    if (jtile && a >= H && a < H + TI && ri0 + a < t.nx) fl[q] |= 1u << 31;  // tile point
+    const int64_t lin = base + (int64_t)li[q] * t.ny + j;
+    sLE[k] = static_cast<const float*>(t.l[0])[lin];
+    sLX[k] = static_cast<const float*>(t.l[1])[lin];
+    sLY[k] = static_cast<const float*>(t.l[2])[lin];
+    if (fl[q] & kTmzPsiE) {
+      sP[k] = static_cast<const float*>(t.phi[rb][0])[lin];
+      sP[NP + k] = static_cast<const float*>(t.phi[rb][1])[lin];
+    }
+    if (fl[q] & kTmzPsiX) sP[2 * NP + k] = static_cast<const float*>(t.phi[rb][2])[lin];
+    if (fl[q] & kTmzPsiY) sP[3 * NP + k] = static_cast<const float*>(t.phi[rb][3])[lin];
+  }
+  unsigned any = 0;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) any |= fl[q];
+  const bool src_e = __syncthreads_or(any & kTmzSrcE) != 0;  // also orders the loads
+  const bool src_h = __syncthreads_or(any & kTmzSrcH) != 0;
+  const int64_t nd = (int64_t)t.dn[0] * t.dn[1];
+  for (int s = nsub - 1; s >= 0; --s) {
+    const int n = n0 + s + 1;
+    if (src_h) {
+      tb_sources<true>(t, 1, n, ri0, rj0, RI, RJ, sLE, sLX, sLY);
+      __syncthreads();
+    }
+    // H half: the curl weight of every Hx / Hy point, then lambda_E gathers
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int k = (ty + kTbRows * q) * RJ + c;
+      sW1[k] = (fl[q] & kTmzPlainX)
+                   ? pt[q].cxn * sLX[k]
+                   : adj_x<P, true>(g, li[q], j, sLX + k, sP + 2 * NP + k, sP + 2 * NP + k);
+      sW2[k] = (fl[q] & kTmzPlainY)
+                   ? pt[q].cy * sLY[k]
+                   : adj_y<P, true>(g, li[q], j, sLY + k, sP + 3 * NP + k, sP + 3 * NP + k);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int a = ty + kTbRows * q, k = a * RJ + c;
+      if (a >= 1 && c >= 1) {
+        float le = sLE[k];
+        if (fl[q] & kTmzMonitor) {
+          bool has;
+          le = le + P::from_double(seed_of(g, t, b, li[q], j, n, &has));
+        }
+        sLE[k] = le + ((sW1[k - 1] - sW1[k]) + (sW2[k - RJ] - sW2[k]));
+      }
+    }
+    __syncthreads();
+    if (src_e) {
+      tb_sources<true>(t, 0, n, ri0, rj0, RI, RJ, sLE, sLX, sLY);
+      __syncthreads();
+    }
+    // E half: the curl weights of every Ez point (and the gradient on tile
+    // design pixels), then lambda_X / lambda_Y gather them
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int k = (ty + kTbRows * q) * RJ + c;
+      float w1, w2;
+      if (fl[q] & kTmzPlainE) {
+        const float le = sLE[k];
+        w1 = pt[q].c1 * le;
+        w2 = pt[q].c2n * le;
+      } else {
+        adj_e<P, true, true, true>(g, t, b, li[q], j, sLE + k, sP + k, sP + k, sP + NP + k,
+                                   sP + NP + k, w1, w2);
+      }
+      sW1[k] = w1;
+      sW2[k] = w2;
+      if ((fl[q] & kTmzDesign) && (fl[q] >> 31)) {
+        const int64_t kk = (int64_t)b * nd + design_index(t, li[q], j);
+        const double le = (double)sLE[k];
+        const double inc = (double)static_cast<const float*>(
+            t.hist)[((int64_t)(n - step0 - 1) * t.nb + b) * nd + (kk - (int64_t)b * nd)];
+        t.grad[kk] += le * inc * t.dc[kk].neg_reps;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int a = ty + kTbRows * q, k = a * RJ + c;
+      if (a < RI - 1 && c < RJ - 1) {
+        sLX[k] = sLX[k] + (sW2[k] - sW2[k + 1]);
+        sLY[k] = sLY[k] + (sW1[k] - sW1[k + RJ]);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    if (!(fl[q] >> 31)) continue;
+    const int k = (ty + kTbRows * q) * RJ + c;
+    const int64_t lin = base + (int64_t)li[q] * t.ny + j;
+    static_cast<float*>(t.tmp[0])[lin] = sLE[k];
+    static_cast<float*>(t.tmp[1])[lin] = sLX[k];
+    static_cast<float*>(t.tmp[2])[lin] = sLY[k];
+    if (fl[q] & kTmzPsiE) {
+      static_cast<float*>(t.phi[wb][0])[lin] = sP[k];
+      static_cast<float*>(t.phi[wb][1])[lin] = sP[NP + k];
+    }
+    if (fl[q] & kTmzPsiX) static_cast<float*>(t.phi[wb][2])[lin] = sP[2 * NP + k];
+    if (fl[q] & kTmzPsiY) static_cast<float*>(t.phi[wb][3])[lin] = sP[3 * NP + k];
+  }
+}
+
+// Region of both blocked kernels: 32 x 64 points; forward 7 arrays (56 KB),
+// adjoint 9 arrays (72 KB) of shared memory.
+constexpr int kTbFwdRI = kTbRI, kTbAdjRI = kTbRI;
+constexpr size_t kTbFwdSmem = (size_t)7 * kTbFwdRI * kTbRJ * sizeof(float);
+constexpr size_t kTbAdjSmem = (size_t)9 * kTbAdjRI * kTbRJ * sizeof(float);
+
+template <int RI>
+dim3 tb_grid(const TmzDev& t) {
+  using G = TbGeom<RI>;
+  return dim3((unsigned)((t.ny + G::TJ - 1) / G::TJ), (unsigned)((t.nx + G::TI - 1) / G::TI),
+              (unsigned)t.nb);
 }
 
 // ---------------------------------------------------------------------------
@@ -490,21 +1076,131 @@ cudaError_t adjoint(const GridDev& g, const TmzDev& t, int step0, int nsteps, cu
   return cudaGetLastError();
 }
 
+// The blocked kernels read one copy of the state and write the other, so
+// the launches alternate between the state and its scratch copy; with an
+// odd number of launches the state is first copied to the scratch, so that
+// the last launch writes the state.
+void swap_fields(TmzDev& u) {  // forward: state <-> scratch
+  for (int k = 0; k < kTmzState; ++k) {
+    void* f = u.f[k];
+    u.f[k] = u.tmp[k];
+    u.tmp[k] = f;
+  }
+}
+
+void swap_adjoints(TmzDev& u) {  // adjoint: field adjoints <-> scratch
+  for (int k = 0; k < 3; ++k) {
+    void* l = u.l[k];
+    u.l[k] = u.tmp[k];
+    u.tmp[k] = l;
+  }
+}
+
+cudaError_t copy_state(void* const* dst, void* const* src, int n, int64_t bytes, cudaStream_t s) {
+  for (int k = 0; k < n; ++k) {
+    const cudaError_t e = cudaMemcpyAsync(dst[k], src[k], (size_t)bytes, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t forward_blocked(const GridDev& g, const TmzDev& t, int step0, int nsteps, int flags,
+                            int per_launch, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k_tmz_tb_fwd<kTbFwdRI>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kTbFwdSmem);
+  if (e != cudaSuccess) return e;
+  if (t.tmp[0] == nullptr) return cudaErrorInvalidValue;
+  const dim3 grid = tb_grid<kTbFwdRI>(t), block(kTbRJ, kTbRows);
+  const int launches = (nsteps + per_launch - 1) / per_launch;
+  TmzDev u = t;
+  if (launches % 2 == 1) {
+    e = copy_state(t.tmp, t.f, kTmzState, (int64_t)t.nb * t.plane * (int64_t)sizeof(float), s);
+    if (e != cudaSuccess) return e;
+    swap_fields(u);
+  }
+  for (int k = 0; k < nsteps; k += per_launch) {
+    const int m = nsteps - k < per_launch ? nsteps - k : per_launch;
+    k_tmz_tb_fwd<kTbFwdRI><<<grid, block, kTbFwdSmem, s>>>(
+        g, u, step0 + k, m, (flags & GMES_TMZ_RECORD_HIST) ? k : -1,
+        (flags & GMES_TMZ_RECORD_MONITOR) ? 1 : 0);
+    swap_fields(u);
+  }
+  return cudaGetLastError();
+}
+
+// Steps per launch of the blocked adjoint, largest first: odd counts of at
+// most per_launch (see k_tmz_tb_adj).
+int adj_chunk(int remaining, int per_launch) {
+  int m = remaining < per_launch ? remaining : per_launch;
+  if (m % 2 == 0) --m;
+  return m;
+}
+
+cudaError_t adjoint_blocked(const GridDev& g, const TmzDev& t, int step0, int nsteps,
+                            int per_launch, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k_tmz_tb_adj<kTbAdjRI>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kTbAdjSmem);
+  if (e != cudaSuccess) return e;
+  if (t.tmp[0] == nullptr) return cudaErrorInvalidValue;
+  const dim3 grid = tb_grid<kTbAdjRI>(t), block(kTbRJ, kTbRows);
+  int launches = 0;
+  for (int hi = nsteps; hi > 0; hi -= adj_chunk(hi, per_launch)) ++launches;
+  TmzDev u = t;
+  if (launches % 2 == 1) {
+    e = copy_state(t.tmp, t.l, 3, (int64_t)t.nb * t.plane * (int64_t)sizeof(float), s);
+    if (e != cudaSuccess) return e;
+    swap_adjoints(u);
+  }
+  for (int hi = nsteps; hi > 0;) {
+    const int m = adj_chunk(hi, per_launch);
+    k_tmz_tb_adj<kTbAdjRI><<<grid, block, kTbAdjSmem, s>>>(g, u, step0 + hi - m, m, step0);
+    swap_adjoints(u);
+    hi -= m;
+  }
+  return cudaGetLastError();
+}
+
+// Steps per launch for a precision and the caller's request (0: default).
+int steps_per_launch(int precision, int requested) {
+  if (precision != GMES_FP32) return 1;
+  if (requested <= 0) return kTbHalo;
+  return requested < kTbHalo ? requested : kTbHalo;
+}
+
 }  // namespace
 
-cudaError_t launch_tmz_design(const GridDev& g, const TmzDev& t, const double* eps,
-                              cudaStream_t s) {
+cudaError_t launch_tmz_design(int precision, const GridDev& g, const TmzDev& t,
+                              const double* eps, cudaStream_t s) {
   const int64_t n = (int64_t)t.dn[0] * t.dn[1] * t.nb;
   if (n > 0) k_tmz_design<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, t, eps);
+  const unsigned mblocks = (unsigned)((t.plane + 255) / 256);
+  switch (precision) {
+    case GMES_FP64:
+      k_tmz_map<PolF64><<<mblocks, 256, 0, s>>>(g, t);
+      break;
+    case GMES_FP32:
+      k_tmz_map<PolF32><<<mblocks, 256, 0, s>>>(g, t);
+      break;
+    case GMES_DF64:
+      k_tmz_map<PolDF><<<mblocks, 256, 0, s>>>(g, t);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  if (t.nsrc > 0) k_tmz_map_sources<<<(t.nsrc + 127) / 128, 128, 0, s>>>(t);
   return cudaGetLastError();
 }
 
 cudaError_t launch_tmz_forward(int precision, const GridDev& g, const TmzDev& t, int step0,
-                               int nsteps, int flags, cudaStream_t s) {
+                               int nsteps, int flags, int block_steps, cudaStream_t s) {
+  const int per = steps_per_launch(precision, block_steps);
   switch (precision) {
     case GMES_FP64:
       return forward<PolF64>(g, t, step0, nsteps, flags, s);
     case GMES_FP32:
+      if (per > 1) return forward_blocked(g, t, step0, nsteps, flags, per, s);
       return forward<PolF32>(g, t, step0, nsteps, flags, s);
     case GMES_DF64:
       return forward<PolDF>(g, t, step0, nsteps, flags, s);
@@ -514,11 +1210,13 @@ cudaError_t launch_tmz_forward(int precision, const GridDev& g, const TmzDev& t,
 }
 
 cudaError_t launch_tmz_adjoint(int precision, const GridDev& g, const TmzDev& t, int step0,
-                               int nsteps, cudaStream_t s) {
+                               int nsteps, int block_steps, cudaStream_t s) {
+  const int per = steps_per_launch(precision, block_steps);
   switch (precision) {
     case GMES_FP64:
       return adjoint<PolF64>(g, t, step0, nsteps, s);
     case GMES_FP32:
+      if (per > 1) return adjoint_blocked(g, t, step0, nsteps, per, s);
       return adjoint<PolF32>(g, t, step0, nsteps, s);
     case GMES_DF64:
       return adjoint<PolDF>(g, t, step0, nsteps, s);

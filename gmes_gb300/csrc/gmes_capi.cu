@@ -740,8 +740,17 @@ constexpr int32_t kTmzActive = (1 << GMES_EZ) | (1 << GMES_HX) | (1 << GMES_HY);
 
 struct TmzLayout {
   int64_t array;  // bytes of one [nb][nx][ny] array, 256-aligned
-  int64_t state, adjoint, design, hist, monitor, grad;
+  int64_t state, adjoint, design, hist, monitor, grad, scratch;
+  // the design buffer: per-pixel coefficients, then the lattice map's
+  // flags and its four coefficient arrays
+  int64_t design_coef, map_flags, map_coef;
 };
+
+// Whether the FP32 forward and adjoint run the temporally blocked kernels,
+// which need the scratch copy of the state.
+bool tmz_blocked(const gmes_grid_desc& g, const gmes_tmz_batch& b) {
+  return g.precision == GMES_FP32 && b.block_steps != 1;
+}
 
 TmzLayout tmz_layout(const gmes_grid_desc& g, const gmes_tmz_batch& b) {
   TmzLayout L;
@@ -752,10 +761,14 @@ TmzLayout tmz_layout(const gmes_grid_desc& g, const gmes_tmz_batch& b) {
   L.array = align256((int64_t)b.nbatch * plane * es);
   L.state = kTmzState * L.array;
   L.adjoint = kTmzAdjoint * L.array;
-  L.design = align256((int64_t)b.nbatch * nd * (int64_t)sizeof(DesignCoef));
+  L.design_coef = align256((int64_t)b.nbatch * nd * (int64_t)sizeof(DesignCoef));
+  L.map_flags = align256(plane * 4);
+  L.map_coef = align256(plane * es);
+  L.design = L.design_coef + L.map_flags + 4 * L.map_coef;
   L.hist = align256((int64_t)b.hist_steps * b.nbatch * nd * es);
   L.monitor = align256((int64_t)b.nbatch * b.total_steps * nm * 8);
   L.grad = align256((int64_t)b.nbatch * nd * 8);
+  L.scratch = tmz_blocked(g, b) ? L.state : 0;
   return L;
 }
 
@@ -780,10 +793,15 @@ gmes_status check_tmz(const gmes_grid_desc* g, const gmes_tmz_batch* b, bool nee
   }
   if (b->nsrc < 0 || b->total_steps < 1 || b->hist_steps < 0)
     return fail(GMES_ERR_VALUE, "negative nsrc / hist_steps or total_steps < 1");
+  if (b->block_steps < 0 || b->block_steps > GMES_TMZ_MAX_BLOCK_STEPS)
+    return fail(GMES_ERR_VALUE, "block_steps = %d outside [0, %d]", b->block_steps,
+                GMES_TMZ_MAX_BLOCK_STEPS);
   if (need_buffers) {
     if (!b->state || !b->adjoint || !b->design || !b->monitor || !b->grad)
       return fail(GMES_ERR_VALUE, "a batch buffer is NULL");
     if (b->hist_steps > 0 && !b->hist) return fail(GMES_ERR_VALUE, "hist is NULL");
+    if (tmz_blocked(*g, *b) && !b->scratch)
+      return fail(GMES_ERR_VALUE, "scratch is NULL (needed by the FP32 blocked kernels)");
     if (b->nsrc > 0 && (!b->src || !b->src_val))
       return fail(GMES_ERR_VALUE, "nsrc > 0 but src or src_val is NULL");
   }
@@ -809,11 +827,16 @@ TmzDev make_tmz_dev(const gmes_grid_desc& g, const gmes_tmz_batch& b) {
   t.hist_steps = b.hist_steps;
   char* s = static_cast<char*>(b.state);
   for (int k = 0; k < kTmzState; ++k) t.f[k] = s + k * L.array;
+  if (tmz_blocked(g, b))
+    for (int k = 0; k < kTmzState; ++k) t.tmp[k] = static_cast<char*>(b.scratch) + k * L.array;
   char* a = static_cast<char*>(b.adjoint);
   for (int k = 0; k < 3; ++k) t.l[k] = a + k * L.array;
   for (int r = 0; r < 2; ++r)
     for (int k = 0; k < 4; ++k) t.phi[r][k] = a + (3 + 4 * r + k) * L.array;
   t.dc = static_cast<const DesignCoef*>(b.design);
+  const char* map = static_cast<const char*>(b.design) + L.design_coef;
+  t.pflags = reinterpret_cast<const uint32_t*>(map);
+  for (int k = 0; k < 4; ++k) t.pcoef[k] = map + L.map_flags + k * L.map_coef;
   t.hist = b.hist;
   t.mon = b.monitor;
   t.grad = b.grad;
@@ -828,7 +851,7 @@ TmzDev make_tmz_dev(const gmes_grid_desc& g, const gmes_tmz_batch& b) {
 
 extern "C" {
 
-gmes_status gmes_tmz_sizes(const gmes_grid_desc* g, const gmes_tmz_batch* b, int64_t sizes[6]) {
+gmes_status gmes_tmz_sizes(const gmes_grid_desc* g, const gmes_tmz_batch* b, int64_t sizes[7]) {
   gmes_status st = check_tmz(g, b, false);
   if (st != GMES_OK) return st;
   if (sizes == nullptr) return fail(GMES_ERR_VALUE, "sizes is NULL");
@@ -839,6 +862,7 @@ gmes_status gmes_tmz_sizes(const gmes_grid_desc* g, const gmes_tmz_batch* b, int
   sizes[3] = L.hist;
   sizes[4] = L.monitor;
   sizes[5] = L.grad;
+  sizes[6] = L.scratch;
   return GMES_OK;
 }
 
@@ -883,7 +907,7 @@ gmes_status gmes_tmz_set_design(const gmes_grid_desc* g, const gmes_tmz_batch* b
   gmes_status st = check_tmz(g, b, true);
   if (st != GMES_OK) return st;
   if (eps == nullptr) return fail(GMES_ERR_VALUE, "eps is NULL");
-  cudaError_t e = launch_tmz_design(make_grid_dev(*g), make_tmz_dev(*g, *b), eps,
+  cudaError_t e = launch_tmz_design(g->precision, make_grid_dev(*g), make_tmz_dev(*g, *b), eps,
                                     static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching the design kernel");
   return GMES_OK;
@@ -915,7 +939,8 @@ gmes_status gmes_tmz_forward(const gmes_grid_desc* g, const gmes_tmz_batch* b, i
   if ((flags & GMES_TMZ_RECORD_HIST) && nsteps > b->hist_steps)
     return fail(GMES_ERR_VALUE, "%d steps exceed the hist capacity %d", nsteps, b->hist_steps);
   cudaError_t e = launch_tmz_forward(g->precision, make_grid_dev(*g), make_tmz_dev(*g, *b),
-                                     step0, nsteps, flags, static_cast<cudaStream_t>(stream));
+                                     step0, nsteps, flags, b->block_steps,
+                                     static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching the forward kernels");
   return GMES_OK;
 }
@@ -943,7 +968,8 @@ gmes_status gmes_tmz_adjoint(const gmes_grid_desc* g, const gmes_tmz_batch* b, i
   if (nsteps > b->hist_steps)
     return fail(GMES_ERR_VALUE, "%d steps exceed the hist capacity %d", nsteps, b->hist_steps);
   cudaError_t e = launch_tmz_adjoint(g->precision, make_grid_dev(*g), make_tmz_dev(*g, *b),
-                                     step0, nsteps, static_cast<cudaStream_t>(stream));
+                                     step0, nsteps, b->block_steps,
+                                     static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching the adjoint kernels");
   return GMES_OK;
 }

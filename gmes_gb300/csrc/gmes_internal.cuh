@@ -318,6 +318,12 @@ struct TmzDev {
   int32_t m0[2], mn[2];     // monitor box
   int32_t total_steps, hist_steps;
   void* f[kTmzState];       // [nb][nx][ny] each
+  void* tmp[kTmzState];     // scratch copy of the state (blocked kernels), or null
+  // Resolved update of every lattice point, shared by the batch (written by
+  // launch_tmz_design): flags (kTmz* below) and the plain-form coefficients
+  // c1, -c2 (Ez), -c1 (Hx), c2 (Hy) as [nx][ny] arrays of the precision's type.
+  const uint32_t* pflags;
+  const void* pcoef[4];
   void* l[3];
   void* phi[2][4];          // ping-pong buffers of the psi adjoints
   const DesignCoef* dc;     // [nb][nd]
@@ -329,12 +335,24 @@ struct TmzDev {
   const double* src_val;    // [total_steps][2][nsrc]
 };
 
-cudaError_t launch_tmz_design(const GridDev& g, const TmzDev& t, const double* eps,
-                              cudaStream_t s);
+// Flags of the resolved lattice map.  "Plain": the update is
+// F + c1 D1 + c2 D2 with per-point coefficients (dielectric points, design
+// pixels, CPML points outside both of their profiles); "psi": a CPML point
+// inside a profile (keeps psi state); neither: the point is not updated.
+// kTmzSrcE / kTmzSrcH: a point source of the E / H half sits on the point.
+enum : uint32_t {
+  kTmzPlainE = 1, kTmzPlainX = 2, kTmzPlainY = 4,
+  kTmzPsiE = 8, kTmzPsiX = 16, kTmzPsiY = 32,
+  kTmzDesign = 64, kTmzMonitor = 128,
+  kTmzSrcE = 256, kTmzSrcH = 512
+};
+
+cudaError_t launch_tmz_design(int precision, const GridDev& g, const TmzDev& t,
+                              const double* eps, cudaStream_t s);
 cudaError_t launch_tmz_forward(int precision, const GridDev& g, const TmzDev& t, int step0,
-                               int nsteps, int flags, cudaStream_t s);
+                               int nsteps, int flags, int block_steps, cudaStream_t s);
 cudaError_t launch_tmz_adjoint(int precision, const GridDev& g, const TmzDev& t, int step0,
-                               int nsteps, cudaStream_t s);
+                               int nsteps, int block_steps, cudaStream_t s);
 cudaError_t launch_tmz_objective(const GridDev& g, const TmzDev& t, int nsteps, double* J,
                                  cudaStream_t s);
 

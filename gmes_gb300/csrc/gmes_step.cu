@@ -26,10 +26,26 @@ namespace gmes {
 namespace {
 
 constexpr int kThreads = 256;
-#ifndef GMES_MIN_BLOCKS
-#define GMES_MIN_BLOCKS 4
+// Resident blocks per SM the cell kernels' register budget targets.
+// Measured on GB300 (256^3 cube): FP32 runs 8% faster at 5 blocks (48
+// registers) than at 4 (56); 6 and 8 blocks spill and run slower.  FP64
+// and df64 already fill the 64 registers of 4 blocks.  GMES_MIN_BLOCKS
+// overrides every precision (tuning builds).
+#ifdef GMES_MIN_BLOCKS
+template <class P>
+struct MinBlocks {
+  static constexpr int value = GMES_MIN_BLOCKS;
+};
+#else
+template <class P>
+struct MinBlocks {
+  static constexpr int value = 4;
+};
+template <>
+struct MinBlocks<PolF32> {
+  static constexpr int value = 5;
+};
 #endif
-constexpr int kMinBlocks = GMES_MIN_BLOCKS;  // resident blocks per SM the register budget targets
 
 template <int C>
 __device__ __forceinline__ int64_t stride_of(const GridDev& g, int axis) {
@@ -510,7 +526,7 @@ __device__ __forceinline__ void cell_body(const GridDev& g, int i, int j, int k)
 }
 
 template <class P, int SIDE, bool STRICT, bool DISP, int MASK, class I>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
+__global__ void __launch_bounds__(kThreads, MinBlocks<P>::value)
     k_cell(const GridDev g, int bx_log2, int i0) {
   const int bx = 1 << bx_log2;
   const int tx = threadIdx.x & (bx - 1);
@@ -747,7 +763,8 @@ __device__ __forceinline__ int find_job(const I* prefix, int njobs, I v) {
 }
 
 template <class P, int SIDE, bool STRICT, bool DISP>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_multi_cell(const BatchView v, int s) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<P>::value)
+    k_multi_cell(const BatchView v, int s) {
   for (int64_t b = blockIdx.x; b < v.tiles; b += gridDim.x) {
     const int job = find_job<int64_t>(v.tile_prefix, v.njobs, b);
     if (s >= __ldg(v.steps + job)) continue;

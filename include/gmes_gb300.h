@@ -46,7 +46,7 @@
 extern "C" {
 #endif
 
-#define GMES_ABI_VERSION 4
+#define GMES_ABI_VERSION 5
 #define GMES_MAX_CLASSES 256 /* class ids are u8 */
 #define GMES_MAX_PML 4       /* PML materials per grid */
 #define GMES_MAX_POLES 8     /* Drude/Lorentz poles, DCP terms per class */
@@ -439,6 +439,7 @@ gmes_status gmes_write_field(const gmes_grid_desc* g, int32_t comp, const double
  */
 #define GMES_TMZ_RECORD_MONITOR 1 /* forward: write the monitor rows of these steps */
 #define GMES_TMZ_RECORD_HIST 2    /* forward: write the design increments (slot = step - step0 - 1) */
+#define GMES_TMZ_MAX_BLOCK_STEPS 4 /* most steps one launch of the FP32 kernels advances */
 
 typedef struct {
   int32_t nbatch;        /* designs */
@@ -449,24 +450,32 @@ typedef struct {
   int32_t nsrc;          /* point sources: comp 2 (Ez), 3 (Hx), 4 (Hy); offset = i * ny + j */
   int32_t total_steps;   /* rows of monitor and src_val */
   int32_t hist_steps;    /* capacity of hist in steps (one checkpoint segment) */
+  int32_t block_steps;   /* FP32: steps per launch, 0 = GMES_TMZ_MAX_BLOCK_STEPS (temporally
+                            blocked kernels), 1 = one step per launch; the results are
+                            bit-identical for every value.  Other precisions: one step. */
   /* device buffers (sizes from gmes_tmz_sizes) */
   void* state;           /* 7 arrays [nbatch][nx][ny]: Ez, Hx, Hy and the 4 CPML psi */
   void* adjoint;         /* 11 arrays: adjoints of Ez, Hx, Hy and 2 x 4 psi adjoints */
-  void* design;          /* per-pixel coefficients, written by gmes_tmz_set_design */
+  void* design;          /* per-pixel coefficients and each lattice point's resolved update,
+                            written by gmes_tmz_set_design */
   void* hist;            /* [hist_steps][nbatch][design points] Ez increments */
   double* monitor;       /* [nbatch][total_steps][monitor points] */
   double* grad;          /* [nbatch][design points] dJ_b / deps */
   const double* weight;  /* [nbatch] seed scale of each J_b (dL/dJ_b), or NULL for 1 */
   const gmes_point_source* src;
   const double* src_val; /* [total_steps][2][nsrc]: E-half and H-half values */
+  void* scratch;         /* second copy of the state for the temporally blocked kernels,
+                            which read one copy and write the other (size 0 and unused
+                            when every launch takes one step) */
 } gmes_tmz_batch;
 
-/* Bytes of state, adjoint, design, hist, monitor, grad. */
-gmes_status gmes_tmz_sizes(const gmes_grid_desc* g, const gmes_tmz_batch* b, int64_t sizes[6]);
+/* Bytes of state, adjoint, design, hist, monitor, grad, scratch. */
+gmes_status gmes_tmz_sizes(const gmes_grid_desc* g, const gmes_tmz_batch* b, int64_t sizes[7]);
 /* Validate the classes of Ez/Hx/Hy and the design box against the grid's
    coefficient block and class maps (synchronous: copies them to the host). */
 gmes_status gmes_tmz_check(const gmes_grid_desc* g, const gmes_tmz_batch* b);
-/* Design coefficients from eps (device, [nbatch][design points], > 0). */
+/* Design coefficients from eps (device, [nbatch][design points], > 0), and
+   the resolved update of every lattice point (flags and coefficients). */
 gmes_status gmes_tmz_set_design(const gmes_grid_desc* g, const gmes_tmz_batch* b,
                                 const double* eps, void* stream);
 /* Zero the state (what & 1) and/or the adjoint and grad (what & 2). */

@@ -123,13 +123,29 @@ def _tmz(**kw):
 def test_tmz_sizes_and_validation():
     lib = N.load()
     d = _desc(n=(16, 12, 1), active=(1 << 2) | (1 << 3) | (1 << 4))
-    sizes = (C.c_int64 * 6)()
+    sizes = (C.c_int64 * 7)()
     N.check(lib.gmes_tmz_sizes(C.byref(d), C.byref(_tmz()), sizes))
     arr = ((2 * 16 * 12 * 8 + 255) // 256) * 256
     assert sizes[0] == 7 * arr and sizes[1] == 11 * arr
-    assert sizes[2] == ((2 * 20 * 48 + 255) // 256) * 256   # DesignCoef = 48 bytes
+    up = lambda v: ((v + 255) // 256) * 256
+    # DesignCoef = 48 bytes per pixel, then the lattice map: flags + 4 coefficient arrays
+    assert sizes[2] == up(2 * 20 * 48) + up(16 * 12 * 4) + 4 * up(16 * 12 * 8)
     assert sizes[3] == ((4 * 2 * 20 * 8 + 255) // 256) * 256
     assert sizes[4] == ((2 * 10 * 4 * 8 + 255) // 256) * 256
+    assert sizes[6] == 0                                     # FP64: one step per launch
+    d32 = _desc(n=(16, 12, 1), active=(1 << 2) | (1 << 3) | (1 << 4))
+    d32.precision = N.FP32
+    N.check(lib.gmes_tmz_sizes(C.byref(d32), C.byref(_tmz()), sizes))
+    arr32 = ((2 * 16 * 12 * 4 + 255) // 256) * 256
+    assert sizes[0] == 7 * arr32 and sizes[6] == 7 * arr32  # blocked kernels: scratch state
+    one = _tmz()
+    one.block_steps = 1
+    N.check(lib.gmes_tmz_sizes(C.byref(d32), C.byref(one), sizes))
+    assert sizes[6] == 0
+    bad = _tmz()
+    bad.block_steps = 5
+    with pytest.raises(ValueError):
+        N.check(lib.gmes_tmz_sizes(C.byref(d32), C.byref(bad), sizes))
     with pytest.raises(IndexError):
         N.check(lib.gmes_tmz_sizes(C.byref(d), C.byref(_tmz(design=((14, 3), (4, 5)))), sizes))
     with pytest.raises(ValueError):

@@ -137,6 +137,42 @@ def test_designs_are_independent_in_a_batch(precision):
     assert np.array_equal(g1[0], g3[1])
 
 
+@pytest.mark.parametrize("n,nsteps,segment,hard", [(48, 160, 7, False), (48, 37, None, True),
+                                                   (130, 161, 9, False)])
+def test_blocked_fp32_kernels_match_one_step_kernels(n, nsteps, segment, hard):
+    """The temporally blocked FP32 kernels (2..4 steps per launch) against
+    the one-step kernels: monitor objective, fields and gradients
+    bit-identical.  The 48^2 lattice is smaller than a block's region (its
+    periodic images repeat inside it); 130^2 has partial edge tiles; the
+    step counts are not multiples of the steps per launch or the segment."""
+    from gmes_gb300.adjoint import TMzAdjoint
+    space, geom, src, design, monitor, eps, ns = problem(hard=hard, batch=2, n=n, nsteps=nsteps,
+                                                         seed=4)
+    out = {}
+    for bs in (1, 2, 3, 4):
+        prob = TMzAdjoint(space, geom, src, design, monitor, ns, batch=2, precision="fp32",
+                          segment=segment, block_steps=bs)
+        J = prob.forward(eps).cpu().numpy()
+        fields = [prob.lattice(k).cpu().numpy() for k in range(3)]
+        g = prob.backward().cpu().numpy()
+        out[bs] = (J, fields, g)
+    J1, f1, g1 = out[1]
+    assert np.all(np.isfinite(g1)) and np.abs(g1).max() > 0
+    for bs in (2, 3, 4):
+        J, f, g = out[bs]
+        assert np.array_equal(J, J1), bs
+        for a, b in zip(f, f1):
+            assert np.array_equal(a, b), bs
+        assert np.array_equal(g, g1), bs
+
+
+def test_block_steps_out_of_range():
+    from gmes_gb300.adjoint import TMzAdjoint
+    space, geom, src, design, monitor, eps, ns = problem()
+    with pytest.raises(ValueError):
+        TMzAdjoint(space, geom, src, design, monitor, ns, precision="fp32", block_steps=5)
+
+
 @pytest.mark.parametrize("precision,tol", [("df64", 1e-9), ("fp32", 1e-5)])
 def test_reduced_precision_gradient_error(precision, tol):
     ref, eps, _ = make("fp64")
