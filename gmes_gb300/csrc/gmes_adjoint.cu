@@ -129,200 +129,134 @@ __device__ __forceinline__ Prof prof_y(const GridDev& g, int pm, int i, int j) {
 }
 
 // ---------------------------------------------------------------------------
-// Per-point forward updates.
+// CPML points inside a profile.
 // ---------------------------------------------------------------------------
-// New Ez of lattice point (i, j) of design b from its value e and curl
-// differences D1 = Y(i,j) - Y(i-1,j), D2 = X(i,j) - X(i,j-1): design pixels
-// with the design's own c1, c2, other points with their Dielectric or CPML
-// updater (other classes keep e).  s1, s2 point at the point's two psi
-// values, read and written only where their CPML profile is on.  *dp gets
-// the design index (-1 off the design) and, on design pixels, *inc the
-// increment c1 D1 - c2 D2.
+// Their updates are those of the reference's CPML updaters
+// (src/pw_cpml.hh:211-237, 319-397) with psi:
+//   Ez: psi1' = b1 psi1 + c1 D1 (where profile 1 is on), likewise psi2;
+//       Ez' = Ez + cdt ((psi1' - psi2') + k1 D1 - k2 D2)
+//   Hx: psi' = b psi + c D1 (on);  Hx' = Hx - cdt (psi' + k D1)
+//   Hy: psi' = b psi + c D2 (on);  Hy' = Hy - cdt (-psi' - k D2)
+// with b, c, k the profile row (entries 0, 3, 4) at the point's index along
+// the profile's axis.  The map (k_tmz_map) holds the class's cdt in the
+// point's coefficient slot, the profile set in the flags' pml fields and
+// which profiles are on, so no class look-up is needed here.
 template <class P>
-__device__ __forceinline__ typename P::R e_point(const GridDev& g, const TmzDev& t, int b, int i,
-                                                 int j, typename P::R e, typename P::R D1,
-                                                 typename P::R D2, typename P::T* s1,
-                                                 typename P::T* s2, int64_t* dp,
-                                                 typename P::R* inc) {
+__device__ __forceinline__ typename P::R e_cpml(const GridDev& g, unsigned fl, typename P::R cdt,
+                                                int i, int j, typename P::R e, typename P::R D1,
+                                                typename P::R D2, typename P::T* s1,
+                                                typename P::T* s2) {
   using R = typename P::R;
-  const int64_t d = design_index(t, i, j);
-  *dp = d;
-  if (d >= 0) {
-    const DesignCoef* dc = t.dc + (int64_t)b * t.dn[0] * t.dn[1] + d;
-    const R c1 = P::cfg(&dc->c1), c2 = P::cfg(&dc->c2);
-    *inc = fmadd(-(c2 * D2), c1, D1);
-    return fmadd(fmadd(e, c1, D1), -c2, D2);
-  }
-  const ClassCoef& cc = class_e(g, i, j);
-  const int kind = __ldg(&cc.kind);
-  if (kind == GMES_KIND_DIELECTRIC)
-    return fmadd(fmadd(e, P::cfg(&cc.c1), D1), -P::cfg(&cc.c2), D2);
-  if (kind != GMES_KIND_CPML) return e;
-  const Prof q = prof_e(g, __ldg(&cc.pml), i, j);
-  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-  if (!on1 && !on2) return fmadd(fmadd(e, P::cfg(&cc.c1), D1), -P::cfg(&cc.c2), D2);
+  const int pm = (fl >> kTmzPmlE) & 3;
+  const Coef* q1 = g.prof[pm][2][0] + (int64_t)i * kProfStride;
+  const Coef* q2 = g.prof[pm][2][1] + (int64_t)j * kProfStride;
   R psi1 = P::ldw(s1), psi2 = P::ldw(s2);
-  if (on1) {
-    psi1 = fmadd(P::cfg(q.q1) * psi1, P::cfg(q.q1 + 3), D1);
+  if (fl & kTmzOnE1) {
+    psi1 = fmadd(P::cfg(q1) * psi1, P::cfg(q1 + 3), D1);
     P::st(s1, psi1);
   }
-  if (on2) {
-    psi2 = fmadd(P::cfg(q.q2) * psi2, P::cfg(q.q2 + 3), D2);
+  if (fl & kTmzOnE2) {
+    psi2 = fmadd(P::cfg(q2) * psi2, P::cfg(q2 + 3), D2);
     P::st(s2, psi2);
   }
-  const R xv = fmadd(fmadd(psi1 - psi2, P::cfg(q.q1 + 4), D1), -P::cfg(q.q2 + 4), D2);
-  return fmadd(e, P::cfg(&cc.cdt), xv);
+  const R xv = fmadd(fmadd(psi1 - psi2, P::cfg(q1 + 4), D1), -P::cfg(q2 + 4), D2);
+  return fmadd(e, cdt, xv);
 }
 
-// New Hx of lattice point (i, j) from its value x and D1 = E(i,j+1) - E(i,j);
-// s: its psi.
 template <class P>
-__device__ __forceinline__ typename P::R x_point(const GridDev& g, int i, int j, typename P::R x,
-                                                 typename P::R dx, typename P::T* s) {
+__device__ __forceinline__ typename P::R x_cpml(const GridDev& g, unsigned fl, typename P::R cdt,
+                                                int j, typename P::R x, typename P::R dx,
+                                                typename P::T* s) {
   using R = typename P::R;
-  const ClassCoef& cc = class_x(g, i, j);
-  const int kind = __ldg(&cc.kind);
-  if (kind == GMES_KIND_DIELECTRIC) return fmadd(x, -P::cfg(&cc.c1), dx);
-  if (kind != GMES_KIND_CPML) return x;
-  const Prof q = prof_x(g, __ldg(&cc.pml), i, j);
-  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-  if (!on1 && !on2) return fmadd(x, -P::cfg(&cc.c1), dx);
+  const Coef* q = g.prof[(fl >> kTmzPmlX) & 3][3][1] + (int64_t)(j + 1) * kProfStride;
   R psi = P::ldw(s);
-  if (on1) {
-    psi = fmadd(P::cfg(q.q1) * psi, P::cfg(q.q1 + 3), dx);
+  if (fl & kTmzOnX) {
+    psi = fmadd(P::cfg(q) * psi, P::cfg(q + 3), dx);
     P::st(s, psi);
   }
-  return fmadd(x, -P::cfg(&cc.cdt), fmadd(psi, P::cfg(q.q1 + 4), dx));
+  return fmadd(x, -cdt, fmadd(psi, P::cfg(q + 4), dx));
 }
 
-// New Hy of lattice point (i, j) from its value y and D2 = E(i+1,j) - E(i,j);
-// s: its psi.
 template <class P>
-__device__ __forceinline__ typename P::R y_point(const GridDev& g, int i, int j, typename P::R y,
-                                                 typename P::R dy, typename P::T* s) {
+__device__ __forceinline__ typename P::R y_cpml(const GridDev& g, unsigned fl, typename P::R cdt,
+                                                int i, typename P::R y, typename P::R dy,
+                                                typename P::T* s) {
   using R = typename P::R;
-  const ClassCoef& cc = class_y(g, i, j);
-  const int kind = __ldg(&cc.kind);
-  if (kind == GMES_KIND_DIELECTRIC) return fmadd(y, P::cfg(&cc.c2), dy);
-  if (kind != GMES_KIND_CPML) return y;
-  const Prof q = prof_y(g, __ldg(&cc.pml), i, j);
-  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-  if (!on1 && !on2) return fmadd(y, P::cfg(&cc.c2), dy);
+  const Coef* q = g.prof[(fl >> kTmzPmlY) & 3][4][0] + (int64_t)(i + 1) * kProfStride;
   R psi = P::ldw(s);
-  if (on2) {
-    psi = fmadd(P::cfg(q.q2) * psi, P::cfg(q.q2 + 3), dy);
+  if (fl & kTmzOnY) {
+    psi = fmadd(P::cfg(q) * psi, P::cfg(q + 3), dy);
     P::st(s, psi);
   }
-  return fmadd(y, -P::cfg(&cc.cdt), fmadd(-psi, -P::cfg(q.q2 + 4), dy));
+  return fmadd(y, -cdt, fmadd(-psi, -P::cfg(q + 4), dy));
 }
 
-// ---------------------------------------------------------------------------
-// Per-point adjoint curl weights.
-// ---------------------------------------------------------------------------
-// Curl weight of the Hx point (i, j): lambda_D1 = dX'/dD1 applied to its
-// adjoint *lxp, with D1 = E(i, j+1) - E(i, j).  phr: its psi adjoint before
-// this step; OWN: the advanced psi adjoint is written to *phw.
+// Their transposes.  Curl weight of an Hx point: lambda_D1 = dX'/dD1
+// applied to its adjoint lx; phr: its psi adjoint before this step, OWN:
+// the advanced one is written to *phw.
 template <class P, bool OWN>
-__device__ __forceinline__ typename P::R adj_x(const GridDev& g, int i, int j,
-                                               const typename P::T* lxp,
-                                               const typename P::T* phr, typename P::T* phw) {
+__device__ __forceinline__ typename P::R adjx_cpml(const GridDev& g, unsigned fl,
+                                                   typename P::R cdt, int j, typename P::R lx,
+                                                   const typename P::T* phr,
+                                                   typename P::T* phw) {
   using R = typename P::R;
-  const ClassCoef& cc = class_x(g, i, j);
-  const int kind = __ldg(&cc.kind);
-  if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return P::zero();
-  const R lx = P::ldw(lxp);
-  if (kind == GMES_KIND_DIELECTRIC) return -(P::cfg(&cc.c1) * lx);
-  const Prof q = prof_x(g, __ldg(&cc.pml), i, j);
-  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-  if (!on1 && !on2) return -(P::cfg(&cc.c1) * lx);
-  const R cdt = P::cfg(&cc.cdt);
-  const R direct = -(cdt * (P::cfg(q.q1 + 4) * lx));
-  if (!on1) return direct;
+  const Coef* q = g.prof[(fl >> kTmzPmlX) & 3][3][1] + (int64_t)(j + 1) * kProfStride;
+  const R direct = -(cdt * (P::cfg(q + 4) * lx));
+  if (!(fl & kTmzOnX)) return direct;
   const R L = fmadd(P::ldw(phr), -cdt, lx);
-  if (OWN) P::st(phw, P::cfg(q.q1) * L);
-  return fmadd(direct, P::cfg(q.q1 + 3), L);
+  if (OWN) P::st(phw, P::cfg(q) * L);
+  return fmadd(direct, P::cfg(q + 3), L);
 }
 
-// Curl weight of the Hy point (i, j): lambda_D2, D2 = E(i+1, j) - E(i, j).
+// Curl weight of an Hy point: lambda_D2, D2 = E(i+1, j) - E(i, j).
 template <class P, bool OWN>
-__device__ __forceinline__ typename P::R adj_y(const GridDev& g, int i, int j,
-                                               const typename P::T* lyp,
-                                               const typename P::T* phr, typename P::T* phw) {
+__device__ __forceinline__ typename P::R adjy_cpml(const GridDev& g, unsigned fl,
+                                                   typename P::R cdt, int i, typename P::R ly,
+                                                   const typename P::T* phr,
+                                                   typename P::T* phw) {
   using R = typename P::R;
-  const ClassCoef& cc = class_y(g, i, j);
-  const int kind = __ldg(&cc.kind);
-  if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return P::zero();
-  const R ly = P::ldw(lyp);
-  if (kind == GMES_KIND_DIELECTRIC) return P::cfg(&cc.c2) * ly;
-  const Prof q = prof_y(g, __ldg(&cc.pml), i, j);
-  const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-  if (!on1 && !on2) return P::cfg(&cc.c2) * ly;
-  const R cdt = P::cfg(&cc.cdt);
-  const R direct = cdt * (P::cfg(q.q2 + 4) * ly);
-  if (!on2) return direct;
+  const Coef* q = g.prof[(fl >> kTmzPmlY) & 3][4][0] + (int64_t)(i + 1) * kProfStride;
+  const R direct = cdt * (P::cfg(q + 4) * ly);
+  if (!(fl & kTmzOnY)) return direct;
   const R L = fmadd(P::ldw(phr), cdt, ly);
-  if (OWN) P::st(phw, P::cfg(q.q2) * L);
-  return fmadd(direct, P::cfg(q.q2 + 3), L);
+  if (OWN) P::st(phw, P::cfg(q) * L);
+  return fmadd(direct, P::cfg(q + 3), L);
 }
 
-// Curl weights (lambda_D1, lambda_D2) of the Ez point (i, j) of design b
-// from its adjoint *lep; phr0/phr1: its two psi adjoints before this step,
-// OWN: the advanced ones are written to *phw0/*phw1.  NEED1/NEED2: which
-// weights the caller uses (both when OWN).
+// Curl weights (lambda_D1, lambda_D2) of an Ez point from its adjoint le;
+// NEED1/NEED2: which weights the caller uses (both when OWN).
 template <class P, bool OWN, bool NEED1, bool NEED2>
-__device__ __forceinline__ void adj_e(const GridDev& g, const TmzDev& t, int b, int i, int j,
-                                      const typename P::T* lep, const typename P::T* phr0,
-                                      typename P::T* phw0, const typename P::T* phr1,
-                                      typename P::T* phw1, typename P::R& w1,
-                                      typename P::R& w2) {
+__device__ __forceinline__ void adje_cpml(const GridDev& g, unsigned fl, typename P::R cdt, int i,
+                                          int j, typename P::R le, const typename P::T* phr0,
+                                          typename P::T* phw0, const typename P::T* phr1,
+                                          typename P::T* phw1, typename P::R& w1,
+                                          typename P::R& w2) {
   using R = typename P::R;
+  const int pm = (fl >> kTmzPmlE) & 3;
   w1 = P::zero();
   w2 = P::zero();
-  const int64_t dp = design_index(t, i, j);
-  R c1, c2;
-  if (dp >= 0) {
-    const DesignCoef* dc = t.dc + (int64_t)b * t.dn[0] * t.dn[1] + dp;
-    c1 = P::cfg(&dc->c1);
-    c2 = P::cfg(&dc->c2);
-  } else {
-    const ClassCoef& cc = class_e(g, i, j);
-    const int kind = __ldg(&cc.kind);
-    if (kind != GMES_KIND_DIELECTRIC && kind != GMES_KIND_CPML) return;
-    c1 = P::cfg(&cc.c1);
-    c2 = P::cfg(&cc.c2);
-    if (kind == GMES_KIND_CPML) {
-      const Prof q = prof_e(g, __ldg(&cc.pml), i, j);
-      const bool on1 = coef_nonzero(q.q1 + 1), on2 = coef_nonzero(q.q2 + 1);
-      if (on1 || on2) {
-        const R le = P::ldw(lep);
-        const R cdt = P::cfg(&cc.cdt);
-        if (NEED1 || OWN) {
-          const R direct = cdt * (P::cfg(q.q1 + 4) * le);
-          if (on1) {
-            const R L = fmadd(P::ldw(phr0), cdt, le);
-            if (OWN) P::st(phw0, P::cfg(q.q1) * L);
-            w1 = fmadd(direct, P::cfg(q.q1 + 3), L);
-          } else {
-            w1 = direct;
-          }
-        }
-        if (NEED2 || OWN) {
-          const R direct = -(cdt * (P::cfg(q.q2 + 4) * le));
-          if (on2) {
-            const R L = fmadd(P::ldw(phr1), -cdt, le);
-            if (OWN) P::st(phw1, P::cfg(q.q2) * L);
-            w2 = fmadd(direct, P::cfg(q.q2 + 3), L);
-          } else {
-            w2 = direct;
-          }
-        }
-        return;
-      }
+  if (NEED1 || OWN) {
+    const Coef* q1 = g.prof[pm][2][0] + (int64_t)i * kProfStride;
+    const R direct = cdt * (P::cfg(q1 + 4) * le);
+    if (fl & kTmzOnE1) {
+      const R L = fmadd(P::ldw(phr0), cdt, le);
+      if (OWN) P::st(phw0, P::cfg(q1) * L);
+      w1 = fmadd(direct, P::cfg(q1 + 3), L);
+    } else {
+      w1 = direct;
     }
   }
-  const R le = P::ldw(lep);
-  if (NEED1 || OWN) w1 = c1 * le;
-  if (NEED2 || OWN) w2 = -(c2 * le);
+  if (NEED2 || OWN) {
+    const Coef* q2 = g.prof[pm][2][1] + (int64_t)j * kProfStride;
+    const R direct = -(cdt * (P::cfg(q2 + 4) * le));
+    if (fl & kTmzOnE2) {
+      const R L = fmadd(P::ldw(phr1), -cdt, le);
+      if (OWN) P::st(phw1, P::cfg(q2) * L);
+      w2 = fmadd(direct, P::cfg(q2 + 3), L);
+    } else {
+      w2 = direct;
+    }
+  }
 }
 
 // Objective seed of lattice point (i, j) of design b at reverse step n:
@@ -353,10 +287,11 @@ __device__ __forceinline__ const typename P::T* map_coef(const TmzDev& t, int k)
 
 // Flags and plain-form coefficients of every lattice point, built once per
 // design set from the class maps, class table and CPML profiles.  The
-// coefficients are the values the per-point functions read (c1, c2 of a
-// Dielectric class, or of a CPML class outside both profiles), so the
-// plain form reproduces them bit for bit.  Design pixels take their
-// coefficients from the per-design table.
+// coefficients are c1, c2 of a Dielectric class, or of a CPML class outside
+// both profiles (whose update reduces to the dielectric form).  Design
+// pixels take theirs from the per-design table.  CPML points inside a
+// profile keep their class's cdt in the coefficient slot, and the flags
+// name the profile set and which of the point's profiles are on.
 template <class P>
 __global__ void k_tmz_map(const GridDev g, const TmzDev t) {
   using R = typename P::R;
@@ -371,8 +306,13 @@ __global__ void k_tmz_map(const GridDev g, const TmzDev t) {
   } else {
     const ClassCoef& cc = class_e(g, i, j);
     const int kind = __ldg(&cc.kind);
-    if (kind == GMES_KIND_CPML && profile_on(prof_e(g, __ldg(&cc.pml), i, j))) {
-      f |= kTmzPsiE;
+    const int pm = __ldg(&cc.pml);
+    if (kind == GMES_KIND_CPML && profile_on(prof_e(g, pm, i, j))) {
+      const Prof q = prof_e(g, pm, i, j);
+      f |= kTmzPsiE | ((unsigned)pm << kTmzPmlE);
+      if (coef_nonzero(q.q1 + 1)) f |= kTmzOnE1;
+      if (coef_nonzero(q.q2 + 1)) f |= kTmzOnE2;
+      c1 = P::cfg(&cc.cdt);
     } else if (kind == GMES_KIND_DIELECTRIC || kind == GMES_KIND_CPML) {
       f |= kTmzPlainE;
       c1 = P::cfg(&cc.c1);
@@ -382,8 +322,11 @@ __global__ void k_tmz_map(const GridDev g, const TmzDev t) {
   {
     const ClassCoef& cc = class_x(g, i, j);
     const int kind = __ldg(&cc.kind);
-    if (kind == GMES_KIND_CPML && profile_on(prof_x(g, __ldg(&cc.pml), i, j))) {
-      f |= kTmzPsiX;
+    const int pm = __ldg(&cc.pml);
+    if (kind == GMES_KIND_CPML && profile_on(prof_x(g, pm, i, j))) {
+      f |= kTmzPsiX | ((unsigned)pm << kTmzPmlX);
+      if (coef_nonzero(prof_x(g, pm, i, j).q1 + 1)) f |= kTmzOnX;
+      cxn = P::cfg(&cc.cdt);
     } else if (kind == GMES_KIND_DIELECTRIC || kind == GMES_KIND_CPML) {
       f |= kTmzPlainX;
       cxn = -P::cfg(&cc.c1);
@@ -392,8 +335,11 @@ __global__ void k_tmz_map(const GridDev g, const TmzDev t) {
   {
     const ClassCoef& cc = class_y(g, i, j);
     const int kind = __ldg(&cc.kind);
-    if (kind == GMES_KIND_CPML && profile_on(prof_y(g, __ldg(&cc.pml), i, j))) {
-      f |= kTmzPsiY;
+    const int pm = __ldg(&cc.pml);
+    if (kind == GMES_KIND_CPML && profile_on(prof_y(g, pm, i, j))) {
+      f |= kTmzPsiY | ((unsigned)pm << kTmzPmlY);
+      if (coef_nonzero(prof_y(g, pm, i, j).q2 + 1)) f |= kTmzOnY;
+      cy = P::cfg(&cc.cdt);
     } else if (kind == GMES_KIND_DIELECTRIC || kind == GMES_KIND_CPML) {
       f |= kTmzPlainY;
       cy = P::cfg(&cc.c2);
@@ -431,18 +377,21 @@ __device__ __forceinline__ void e_coef(const TmzDev& t, int b, int i, int j, int
   }
 }
 
-// Adjoint curl weights through the map: the plain form, or the per-point
-// functions on CPML points inside a profile.  ll: lattice offset; base:
-// the design's offset.
+// Adjoint curl weights through the map: the plain form, the CPML form on
+// points inside a profile, zero on points that are not updated.  ll:
+// lattice offset; base: the design's offset.
 template <class P, bool OWN>
 __device__ __forceinline__ typename P::R weight_x(const GridDev& g, const TmzDev& t, int i, int j,
                                                   int64_t ll, int64_t base, int rb, int wb) {
   using T = typename P::T;
   const T* lx = static_cast<const T*>(t.l[1]) + base + ll;
   const typename P::R c = P::ld(map_coef<P>(t, 2) + ll);  // issued with the flags
-  if (__ldg(t.pflags + ll) & kTmzPlainX) return c * P::ldw(lx);
-  return adj_x<P, OWN>(g, i, j, lx, static_cast<const T*>(t.phi[rb][2]) + base + ll,
-                       OWN ? static_cast<T*>(t.phi[wb][2]) + base + ll : nullptr);
+  const unsigned fl = __ldg(t.pflags + ll);
+  if (fl & kTmzPlainX) return c * P::ldw(lx);
+  if (!(fl & kTmzPsiX)) return P::zero();
+  return adjx_cpml<P, OWN>(g, fl, c, j, P::ldw(lx),
+                           static_cast<const T*>(t.phi[rb][2]) + base + ll,
+                           OWN ? static_cast<T*>(t.phi[wb][2]) + base + ll : nullptr);
 }
 
 template <class P, bool OWN>
@@ -451,9 +400,12 @@ __device__ __forceinline__ typename P::R weight_y(const GridDev& g, const TmzDev
   using T = typename P::T;
   const T* ly = static_cast<const T*>(t.l[2]) + base + ll;
   const typename P::R c = P::ld(map_coef<P>(t, 3) + ll);  // issued with the flags
-  if (__ldg(t.pflags + ll) & kTmzPlainY) return c * P::ldw(ly);
-  return adj_y<P, OWN>(g, i, j, ly, static_cast<const T*>(t.phi[rb][3]) + base + ll,
-                       OWN ? static_cast<T*>(t.phi[wb][3]) + base + ll : nullptr);
+  const unsigned fl = __ldg(t.pflags + ll);
+  if (fl & kTmzPlainY) return c * P::ldw(ly);
+  if (!(fl & kTmzPsiY)) return P::zero();
+  return adjy_cpml<P, OWN>(g, fl, c, i, P::ldw(ly),
+                           static_cast<const T*>(t.phi[rb][3]) + base + ll,
+                           OWN ? static_cast<T*>(t.phi[wb][3]) + base + ll : nullptr);
 }
 
 template <class P, bool OWN, bool NEED1, bool NEED2>
@@ -464,18 +416,24 @@ __device__ __forceinline__ void weight_e(const GridDev& g, const TmzDev& t, int 
   using T = typename P::T;
   const T* le = static_cast<const T*>(t.l[0]) + base + ll;
   const unsigned fl = __ldg(t.pflags + ll);
+  R c1, c2n;
+  e_coef<P>(t, b, i, j, ll, fl, c1, c2n);
   if (fl & kTmzPlainE) {
-    R c1, c2n;
-    e_coef<P>(t, b, i, j, ll, fl, c1, c2n);
     const R v = P::ldw(le);
     w1 = c1 * v;
     w2 = c2n * v;
     return;
   }
-  adj_e<P, OWN, NEED1, NEED2>(g, t, b, i, j, le, static_cast<const T*>(t.phi[rb][0]) + base + ll,
-                              OWN ? static_cast<T*>(t.phi[wb][0]) + base + ll : nullptr,
-                              static_cast<const T*>(t.phi[rb][1]) + base + ll,
-                              OWN ? static_cast<T*>(t.phi[wb][1]) + base + ll : nullptr, w1, w2);
+  if (!(fl & kTmzPsiE)) {
+    w1 = w2 = P::zero();
+    return;
+  }
+  adje_cpml<P, OWN, NEED1, NEED2>(g, fl, c1, i, j, P::ldw(le),
+                                  static_cast<const T*>(t.phi[rb][0]) + base + ll,
+                                  OWN ? static_cast<T*>(t.phi[wb][0]) + base + ll : nullptr,
+                                  static_cast<const T*>(t.phi[rb][1]) + base + ll,
+                                  OWN ? static_cast<T*>(t.phi[wb][1]) + base + ll : nullptr, w1,
+                                  w2);
 }
 
 // ---------------------------------------------------------------------------
@@ -506,11 +464,9 @@ __global__ void __launch_bounds__(kBX* kBY) k_tmz_fe(const GridDev g, const TmzD
             fmadd(c2n * D2, c1, D1));
     }
   } else if (fl & kTmzPsiE) {
-    int64_t dp;
-    R inc;
-    P::st(E + p.lin, e_point<P>(g, t, p.b, p.i, p.j, e, D1, D2,
-                                static_cast<T*>(t.f[3]) + p.base + p.lin,
-                                static_cast<T*>(t.f[4]) + p.base + p.lin, &dp, &inc));
+    P::st(E + p.lin, e_cpml<P>(g, fl, P::ld(map_coef<P>(t, 0) + p.lin), p.i, p.j, e, D1, D2,
+                               static_cast<T*>(t.f[3]) + p.base + p.lin,
+                               static_cast<T*>(t.f[4]) + p.base + p.lin));
   }
 }
 
@@ -532,13 +488,13 @@ __global__ void __launch_bounds__(kBX* kBY) k_tmz_fh(const GridDev g, const TmzD
   if (fl & kTmzPlainX)
     P::st(X + p.lin, fmadd(P::ldw(X + p.lin), cxn, dx));
   else if (fl & kTmzPsiX)
-    P::st(X + p.lin, x_point<P>(g, p.i, p.j, P::ldw(X + p.lin), dx,
-                                static_cast<T*>(t.f[5]) + p.base + p.lin));
+    P::st(X + p.lin, x_cpml<P>(g, fl, cxn, p.j, P::ldw(X + p.lin), dx,
+                               static_cast<T*>(t.f[5]) + p.base + p.lin));
   if (fl & kTmzPlainY)
     P::st(Y + p.lin, fmadd(P::ldw(Y + p.lin), cy, dy));
   else if (fl & kTmzPsiY)
-    P::st(Y + p.lin, y_point<P>(g, p.i, p.j, P::ldw(Y + p.lin), dy,
-                                static_cast<T*>(t.f[6]) + p.base + p.lin));
+    P::st(Y + p.lin, y_cpml<P>(g, fl, cy, p.i, P::ldw(Y + p.lin), dy,
+                               static_cast<T*>(t.f[6]) + p.base + p.lin));
   if (row >= 0 && (fl & kTmzMonitor)) {
     const int64_t nm = (int64_t)t.mn[0] * t.mn[1];
     t.mon[((int64_t)p.b * t.total_steps + row) * nm + monitor_index(t, p.i, p.j)] = to_double(e0);
@@ -796,9 +752,7 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
                                         design_index(t, li[q], j)] =
                 fmadd(pt[q].c2n * D2, pt[q].c1, D1);
         } else if (fl[q] & kTmzPsiE) {
-          int64_t dp;
-          float inc;
-          sE[k] = e_point<P>(g, t, b, li[q], j, sE[k], D1, D2, sS + k, sS + NP + k, &dp, &inc);
+          sE[k] = e_cpml<P>(g, fl[q], pt[q].c1, li[q], j, sE[k], D1, D2, sS + k, sS + NP + k);
         }
       }
     }
@@ -816,11 +770,11 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
         if (fl[q] & kTmzPlainX)
           sX[k] = fmadd(sX[k], pt[q].cxn, dx);
         else if (fl[q] & kTmzPsiX)
-          sX[k] = x_point<P>(g, li[q], j, sX[k], dx, sS + 2 * NP + k);
+          sX[k] = x_cpml<P>(g, fl[q], pt[q].cxn, j, sX[k], dx, sS + 2 * NP + k);
         if (fl[q] & kTmzPlainY)
           sY[k] = fmadd(sY[k], pt[q].cy, dy);
         else if (fl[q] & kTmzPsiY)
-          sY[k] = y_point<P>(g, li[q], j, sY[k], dy, sS + 3 * NP + k);
+          sY[k] = y_cpml<P>(g, fl[q], pt[q].cy, li[q], sY[k], dy, sS + 3 * NP + k);
         if (rec_mon && (fl[q] & kTmzMonitor) && (fl[q] >> 31))
           t.mon[((int64_t)b * t.total_steps + (n - 1)) * nm + monitor_index(t, li[q], j)] =
               (double)e0;
@@ -911,12 +865,16 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int k = (ty + kTbRows * q) * RJ + c;
-      sW1[k] = (fl[q] & kTmzPlainX)
-                   ? pt[q].cxn * sLX[k]
-                   : adj_x<P, true>(g, li[q], j, sLX + k, sP + 2 * NP + k, sP + 2 * NP + k);
-      sW2[k] = (fl[q] & kTmzPlainY)
-                   ? pt[q].cy * sLY[k]
-                   : adj_y<P, true>(g, li[q], j, sLY + k, sP + 3 * NP + k, sP + 3 * NP + k);
+      sW1[k] = (fl[q] & kTmzPlainX) ? pt[q].cxn * sLX[k]
+               : (fl[q] & kTmzPsiX)
+                   ? adjx_cpml<P, true>(g, fl[q], pt[q].cxn, j, sLX[k], sP + 2 * NP + k,
+                                        sP + 2 * NP + k)
+                   : 0.f;
+      sW2[k] = (fl[q] & kTmzPlainY) ? pt[q].cy * sLY[k]
+               : (fl[q] & kTmzPsiY)
+                   ? adjy_cpml<P, true>(g, fl[q], pt[q].cy, li[q], sLY[k], sP + 3 * NP + k,
+                                        sP + 3 * NP + k)
+                   : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -947,8 +905,10 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
         w1 = pt[q].c1 * le;
         w2 = pt[q].c2n * le;
       } else {
-        adj_e<P, true, true, true>(g, t, b, li[q], j, sLE + k, sP + k, sP + k, sP + NP + k,
-                                   sP + NP + k, w1, w2);
+        w1 = w2 = 0.f;
+        if (fl[q] & kTmzPsiE)
+          adje_cpml<P, true, true, true>(g, fl[q], pt[q].c1, li[q], j, sLE[k], sP + k, sP + k,
+                                         sP + NP + k, sP + NP + k, w1, w2);
       }
       sW1[k] = w1;
       sW2[k] = w2;

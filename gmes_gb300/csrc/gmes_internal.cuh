@@ -340,12 +340,18 @@ struct TmzDev {
 // pixels, CPML points outside both of their profiles); "psi": a CPML point
 // inside a profile (keeps psi state); neither: the point is not updated.
 // kTmzSrcE / kTmzSrcH: a point source of the E / H half sits on the point.
+// For psi points, kTmzOn*: which of the point's profiles are on (Ez: along
+// x and y; Hx: along y; Hy: along x) and the 2-bit fields at kTmzPml*: the
+// class's profile set.
 enum : uint32_t {
   kTmzPlainE = 1, kTmzPlainX = 2, kTmzPlainY = 4,
   kTmzPsiE = 8, kTmzPsiX = 16, kTmzPsiY = 32,
   kTmzDesign = 64, kTmzMonitor = 128,
-  kTmzSrcE = 256, kTmzSrcH = 512
+  kTmzSrcE = 256, kTmzSrcH = 512,
+  kTmzOnE1 = 1024, kTmzOnE2 = 2048, kTmzOnX = 4096, kTmzOnY = 8192
 };
+constexpr int kTmzPmlE = 16, kTmzPmlX = 18, kTmzPmlY = 20;  // bit offsets
+static_assert(GMES_MAX_PML <= 4, "2-bit profile-set fields");
 
 cudaError_t launch_tmz_design(int precision, const GridDev& g, const TmzDev& t,
                               const double* eps, cudaStream_t s);
