@@ -515,6 +515,9 @@ def run_design(args):
     fwd_gbs = 9 * es * cells * nsteps * args.batch / tf / 1e9
     bwd_gbs = 2 * 9 * es * cells * nsteps * args.batch / tb / 1e9
     peak = measured_peak()
+    per = (args.block_steps or 4) if precision == "fp32" else 1
+    fwd_kernel = (f"forward, k_tmz_tb_fwd ({per} steps per launch)" if per > 1
+                  else "forward, k_tmz_fe + k_tmz_fh")
     result = {
         "metric": METRIC, "value": round(upd / per / 1e9, 4), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": round(per * 1e3, 3),
@@ -531,6 +534,16 @@ def run_design(args):
         "forward_s": round(tf, 4), "backward_s": round(tb, 4),
         "forward_alg_GBps": round(fwd_gbs, 1), "backward_alg_GBps": round(bwd_gbs, 1),
         "hbm_peak_GBps": peak[0] if peak else None,
+        # the forward pass against HBM: algorithmic bytes of a one-step
+        # kernel (9 values per cell-step) per second; traffic = measured DRAM
+        # bytes of one forward launch (ncu), which temporal blocking keeps
+        # well below the algorithmic bytes of the steps it advances
+        "roofline": {"bound": "hbm", "achieved": round(fwd_gbs, 1), "peak": peak[0],
+                     "unit": "GB/s", "frac": round(fwd_gbs / peak[0], 4),
+                     "traffic": ncu_traffic(f"design2d_tmz_{n}x{n}_batch{args.batch}_{per}steps",
+                                            precision),
+                     "alg_bytes_per_launch": 9 * es * cells * args.batch * per,
+                     "kernel": fwd_kernel, "peak_source": peak[1]},
         "wall_s": round(wall, 3), "grad_finite": bool(torch.isfinite(g).all()),
         "clocks": clocks,
         "gpu_launches": args.steps * (design_launches(prob, precision, args.block_steps) + 2),
