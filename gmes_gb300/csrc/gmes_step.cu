@@ -762,13 +762,32 @@ __device__ __forceinline__ int find_job(const I* prefix, int njobs, I v) {
   return lo;
 }
 
+static_assert(sizeof(GridDev) % 16 == 0, "GridDev is copied as 16-byte words");
+
+// The tile's grid descriptor is copied to shared memory when the block's
+// job changes and read from there: read from global memory, its fields
+// (pointers, strides, tables of six components) cost the batched FP32
+// half-step ~70 extra global loads per cell and ran it 1.7x slower than
+// the single-grid kernel, whose descriptor is a kernel parameter; from
+// shared memory it runs 1.3x slower (measured on GB300, 160^3 cube).
 template <class P, int SIDE, bool STRICT, bool DISP>
 __global__ void __launch_bounds__(kThreads, MinBlocks<P>::value)
     k_multi_cell(const BatchView v, int s) {
+  __shared__ __align__(16) unsigned char desc[sizeof(GridDev)];
+  const GridDev& g = *reinterpret_cast<const GridDev*>(desc);
+  int cached = -1;
   for (int64_t b = blockIdx.x; b < v.tiles; b += gridDim.x) {
-    const int job = find_job<int64_t>(v.tile_prefix, v.njobs, b);
+    const int job = find_job<int64_t>(v.tile_prefix, v.njobs, b);  // block-uniform
     if (s >= __ldg(v.steps + job)) continue;
-    const GridDev& g = v.jobs[job];
+    if (job != cached) {
+      __syncthreads();  // the previous descriptor is no longer read
+      const uint4* src = reinterpret_cast<const uint4*>(v.jobs + job);
+      uint4* dst = reinterpret_cast<uint4*>(desc);
+      for (int w = threadIdx.x; w < (int)(sizeof(GridDev) / 16); w += blockDim.x)
+        dst[w] = __ldg(src + w);
+      __syncthreads();
+      cached = job;
+    }
     const int bxl = __ldg(v.bxl + job);
     const int bx = 1 << bxl, by = kThreads >> bxl;
     const int nkb = (g.n[2] + bx - 1) / bx, njb = (g.n[1] + by - 1) / by;
