@@ -297,6 +297,23 @@ def cpu_baseline(sim, seconds, threads=None):
                        f"static loops, {Oracle.threads()} threads")}, nsteps, dt
 
 
+def replica_throughput(total_ms, cells, steps, dist=None, device="cpu"):
+    """(job time in ms, whole-job Gcell-updates/s) of N independent replicas.
+
+    Every rank advanced its own ``cells``-cell grid ``steps`` steps in
+    ``total_ms``; the job takes as long as the slowest rank (max over ranks)
+    and its throughput counts the cell-updates of all ranks.
+    """
+    world = 1
+    if dist is not None:
+        import torch
+        world = dist.get_world_size()
+        t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, cells * steps * world / (total_ms / 1e3) / 1e9
+
+
 def run_ours(args):
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -320,11 +337,7 @@ def run_ours(args):
     clk.start()
     total_ms, e_ms, h_ms, wall = timed_loop(sim, args.steps, args.warmup, rank_sync)
     clocks = clk.stop()
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = cells * args.steps * world / (total_ms / 1e3) / 1e9
+    total_ms, value = replica_throughput(total_ms, cells, args.steps, dist, "cuda")
     eb, hb = half_bytes(scene, args.precision, sim.engine)
     dom = ("E half-step", eb, e_ms) if e_ms >= h_ms else ("H half-step", hb, h_ms)
     peak, peak_src = measured_peak()
