@@ -32,7 +32,7 @@ def _rank(rank, world, port, out):
 
 def test_replica_throughput_takes_the_slowest_rank_and_counts_every_rank():
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of a multi-threaded process
         out = m.dict()
         mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
         res = dict(out)
