@@ -166,6 +166,21 @@ def ncu_traffic(workload_key, precision):
         return None
 
 
+def ncu_pipe(workload_key, precision):
+    """The busiest execution pipe of the dominant kernel (committed ncu summary).
+
+    Where a kernel is bound by an arithmetic pipe rather than by DRAM (the
+    FP64 cell kernel: FP64 pipe), this says which pipe and how busy it was.
+    """
+    p = ROOT / "profiles" / "pipes.json"
+    if not p.exists():
+        return None
+    try:
+        return json.loads(p.read_text()).get(f"{workload_key}/{precision}")
+    except ValueError:
+        return None
+
+
 # ---------------------------------------------------------------------------
 # algorithmic bytes
 # ---------------------------------------------------------------------------
@@ -358,7 +373,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": dom[0], "alg_bytes_per_launch": dom[1],
-                     "launch_ms": round(dom[2], 5), "peak_source": peak_src},
+                     "launch_ms": round(dom[2], 5), "peak_source": peak_src,
+                     "pipe": ncu_pipe(cfg["workload"], args.precision)},
         "half_ms": {"E": round(e_ms, 5), "H": round(h_ms, 5)},
         "gpu_launches": args.steps * (6 if scene.sources else 4),
         "clocks": clocks,
