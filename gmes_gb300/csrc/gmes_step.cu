@@ -29,8 +29,9 @@ constexpr int kThreads = 256;
 // Resident blocks per SM the cell kernels' register budget targets.
 // Measured on GB300 (256^3 cube): FP32 runs 8% faster at 5 blocks (48
 // registers) than at 4 (56); 6 and 8 blocks spill and run slower.  FP64
-// and df64 already fill the 64 registers of 4 blocks.  GMES_MIN_BLOCKS
-// overrides every precision (tuning builds).
+// and df64 run best at 4 (64 registers): at 5 they spill and lose 5% and
+// 12%, at 3 FP64 loses 3%.  GMES_MIN_BLOCKS overrides every precision
+// (tuning builds).
 #ifdef GMES_MIN_BLOCKS
 template <class P>
 struct MinBlocks {
