@@ -80,7 +80,9 @@ def build_sim(args, precision):
         n = args.n or 192
         sim, full_steps = W.dispersive(n=n, precision=precision)
         cfg = {"workload": f"cube{n}_drude_lorentz_dcp_upml", "grid": [n, n, n],
-               "pml_cells": 12, "source": "Bandpass(0.5, 0.2) Ez point (TFSF pending)",
+               "pml_cells": 12,
+               "source": "TFSF plane wave +z, x-polarised, Bandpass(0.5, 0.2), box 90% of the "
+                         "PML-free interior",
                "courant_ratio": 0.6, "job_steps": full_steps}
     else:
         sim, full_steps = W.air2d(precision=precision)
