@@ -546,8 +546,8 @@ def run_design(args):
     fwd_gbs = 9 * es * cells * nsteps * args.batch / tf / 1e9
     bwd_gbs = 2 * 9 * es * cells * nsteps * args.batch / tb / 1e9
     peak = measured_peak()
-    per = (args.block_steps or 4) if precision == "fp32" else 1
-    fwd_kernel = (f"forward, k_tmz_tb_fwd ({per} steps per launch)" if per > 1
+    spl = (args.block_steps or 4) if precision == "fp32" else 1  # steps per forward launch
+    fwd_kernel = (f"forward, k_tmz_tb_fwd ({spl} steps per launch)" if spl > 1
                   else "forward, k_tmz_fe + k_tmz_fh")
     result = {
         "metric": METRIC, "value": round(upd / per / 1e9, 4), "unit": UNIT, "n_gpus": 1,
@@ -571,9 +571,9 @@ def run_design(args):
         # well below the algorithmic bytes of the steps it advances
         "roofline": {"bound": "hbm", "achieved": round(fwd_gbs, 1), "peak": peak[0],
                      "unit": "GB/s", "frac": round(fwd_gbs / peak[0], 4),
-                     "traffic": ncu_traffic(f"design2d_tmz_{n}x{n}_batch{args.batch}_{per}steps",
+                     "traffic": ncu_traffic(f"design2d_tmz_{n}x{n}_batch{args.batch}_{spl}steps",
                                             precision),
-                     "alg_bytes_per_launch": 9 * es * cells * args.batch * per,
+                     "alg_bytes_per_launch": 9 * es * cells * args.batch * spl,
                      "kernel": fwd_kernel, "peak_source": peak[1]},
         "wall_s": round(wall, 3), "grad_finite": bool(torch.isfinite(g).all()),
         "clocks": clocks,
