@@ -1,0 +1,47 @@
+"""The bench's JSON line on small cases: required keys present and the
+figures consistent with each other (value, ms per step, gradients/s,
+roofline fraction)."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def bench(*args):
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], cwd=ROOT,
+                         capture_output=True, text=True, timeout=900)
+    assert out.returncode == 0, out.stderr[-2000:]
+    return json.loads(out.stdout.strip().splitlines()[-1])
+
+
+def test_cube_line():
+    d = bench("--n", "48", "--steps", "5", "--warmup", "3", "--no-cpu-baseline", "--no-variants")
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+                "roofline", "e2e", "clocks", "gpu_launches"):
+        assert key in d, key
+    cells = 48 ** 3
+    assert d["value"] == pytest.approx(cells / (d["ms_per_step"] / 1e3) / 1e9, rel=1e-3)
+    r = d["roofline"]
+    assert r["frac"] == pytest.approx(r["achieved"] / r["peak"], rel=1e-3)
+    assert r["achieved"] == pytest.approx(r["alg_bytes_per_launch"] / (r["launch_ms"] / 1e3) / 1e9,
+                                          rel=1e-2)
+    assert d["e2e"]["h2d_bytes_per_step"] >= 0 and d["e2e"]["value"] > 0
+    assert d["gpu_launches"] > 0
+
+
+def test_design_line():
+    d = bench("--workload", "design2d", "--n", "160", "--batch", "2", "--steps", "1",
+              "--warmup", "1", "--no-cpu-baseline")
+    per = d["forward_s"] + d["backward_s"]
+    assert d["ms_per_step"] == pytest.approx(per * 1e3, rel=1e-3)
+    assert d["gradients_per_s"] == pytest.approx(2 / per, rel=1e-3)
+    cells, steps = 160 * 160, d["config"]["time_steps"]
+    assert d["value"] == pytest.approx(3 * cells * steps * 2 / per / 1e9, rel=1e-3)
+    assert d["grad_finite"]
