@@ -626,6 +626,11 @@ constexpr int kTbHalo = GMES_TMZ_MAX_BLOCK_STEPS;  // most steps per launch
 constexpr int kTbRJ = 64;    // region columns (j)
 constexpr int kTbRows = 8;   // thread rows
 constexpr int kTbThreads = kTbRJ * kTbRows;
+
+template <bool B>
+struct PsiTag {
+  static constexpr bool value = B;
+};
 constexpr int kTbRI = 32;    // region rows (i)
 #ifndef GMES_TB_MIN_BLOCKS
 #define GMES_TB_MIN_BLOCKS 2
@@ -738,54 +743,65 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
   const bool src_h = __syncthreads_or(any & kTmzSrcH) != 0;
   const int64_t nd = (int64_t)t.dn[0] * t.dn[1];
   const int64_t nm = (int64_t)t.mn[0] * t.mn[1];
-  for (int s = 0; s < nsub; ++s) {
-    const int n = n0 + s + 1;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int a = ty + kTbRows * q, k = a * RJ + c;
-      if (a >= 1 && c >= 1) {
-        const float D1 = sY[k] - sY[k - RJ], D2 = sX[k] - sX[k - 1];
-        if (fl[q] & kTmzPlainE) {
-          sE[k] = fmadd(fmadd(sE[k], pt[q].c1, D1), pt[q].c2n, D2);
-          if ((fl[q] & kTmzDesign) && (fl[q] >> 31) && slot0 >= 0)
-            static_cast<float*>(t.hist)[((int64_t)(slot0 + s) * t.nb + b) * nd +
-                                        design_index(t, li[q], j)] =
-                fmadd(pt[q].c2n * D2, pt[q].c1, D1);
-        } else if (fl[q] & kTmzPsiE) {
-          sE[k] = e_cpml<P>(g, fl[q], pt[q].c1, li[q], j, sE[k], D1, D2, sS + k, sS + NP + k);
+  // Regions without CPML points inside a profile (most tiles) run a copy of
+  // the sub-step loop without that code path: the choice is block-uniform,
+  // and the arithmetic of every point is the same in both copies.
+  const bool psi_any = __syncthreads_or(any & (kTmzPsiE | kTmzPsiX | kTmzPsiY)) != 0;
+  auto steps = [&](auto tag) {
+    constexpr bool PSI = decltype(tag)::value;
+    for (int s = 0; s < nsub; ++s) {
+      const int n = n0 + s + 1;
+  #pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int a = ty + kTbRows * q, k = a * RJ + c;
+        if (a >= 1 && c >= 1) {
+          const float D1 = sY[k] - sY[k - RJ], D2 = sX[k] - sX[k - 1];
+          if (fl[q] & kTmzPlainE) {
+            sE[k] = fmadd(fmadd(sE[k], pt[q].c1, D1), pt[q].c2n, D2);
+            if ((fl[q] & kTmzDesign) && (fl[q] >> 31) && slot0 >= 0)
+              static_cast<float*>(t.hist)[((int64_t)(slot0 + s) * t.nb + b) * nd +
+                                          design_index(t, li[q], j)] =
+                  fmadd(pt[q].c2n * D2, pt[q].c1, D1);
+          } else if (PSI && (fl[q] & kTmzPsiE)) {
+            sE[k] = e_cpml<P>(g, fl[q], pt[q].c1, li[q], j, sE[k], D1, D2, sS + k, sS + NP + k);
+          }
         }
       }
-    }
-    __syncthreads();
-    if (src_e) {
-      tb_sources<false>(t, 0, n, ri0, rj0, RI, RJ, sE, sX, sY);
       __syncthreads();
-    }
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int a = ty + kTbRows * q, k = a * RJ + c;
-      if (a < RI - 1 && c < RJ - 1) {
-        const float e0 = sE[k];
-        const float dx = sE[k + 1] - e0, dy = sE[k + RJ] - e0;
-        if (fl[q] & kTmzPlainX)
-          sX[k] = fmadd(sX[k], pt[q].cxn, dx);
-        else if (fl[q] & kTmzPsiX)
-          sX[k] = x_cpml<P>(g, fl[q], pt[q].cxn, j, sX[k], dx, sS + 2 * NP + k);
-        if (fl[q] & kTmzPlainY)
-          sY[k] = fmadd(sY[k], pt[q].cy, dy);
-        else if (fl[q] & kTmzPsiY)
-          sY[k] = y_cpml<P>(g, fl[q], pt[q].cy, li[q], sY[k], dy, sS + 3 * NP + k);
-        if (rec_mon && (fl[q] & kTmzMonitor) && (fl[q] >> 31))
-          t.mon[((int64_t)b * t.total_steps + (n - 1)) * nm + monitor_index(t, li[q], j)] =
-              (double)e0;
+      if (src_e) {
+        tb_sources<false>(t, 0, n, ri0, rj0, RI, RJ, sE, sX, sY);
+        __syncthreads();
+      }
+  #pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int a = ty + kTbRows * q, k = a * RJ + c;
+        if (a < RI - 1 && c < RJ - 1) {
+          const float e0 = sE[k];
+          const float dx = sE[k + 1] - e0, dy = sE[k + RJ] - e0;
+          if (fl[q] & kTmzPlainX)
+            sX[k] = fmadd(sX[k], pt[q].cxn, dx);
+          else if (PSI && (fl[q] & kTmzPsiX))
+            sX[k] = x_cpml<P>(g, fl[q], pt[q].cxn, j, sX[k], dx, sS + 2 * NP + k);
+          if (fl[q] & kTmzPlainY)
+            sY[k] = fmadd(sY[k], pt[q].cy, dy);
+          else if (PSI && (fl[q] & kTmzPsiY))
+            sY[k] = y_cpml<P>(g, fl[q], pt[q].cy, li[q], sY[k], dy, sS + 3 * NP + k);
+          if (rec_mon && (fl[q] & kTmzMonitor) && (fl[q] >> 31))
+            t.mon[((int64_t)b * t.total_steps + (n - 1)) * nm + monitor_index(t, li[q], j)] =
+                (double)e0;
+        }
+      }
+      __syncthreads();
+      if (src_h) {
+        tb_sources<false>(t, 1, n, ri0, rj0, RI, RJ, sE, sX, sY);
+        __syncthreads();
       }
     }
-    __syncthreads();
-    if (src_h) {
-      tb_sources<false>(t, 1, n, ri0, rj0, RI, RJ, sE, sX, sY);
-      __syncthreads();
-    }
-  }
+  };
+  if (psi_any)
+    steps(PsiTag<true>{});
+  else
+    steps(PsiTag<false>{});
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     if (!(fl[q] >> 31)) continue;
@@ -855,82 +871,92 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
   const bool src_e = __syncthreads_or(any & kTmzSrcE) != 0;  // also orders the loads
   const bool src_h = __syncthreads_or(any & kTmzSrcH) != 0;
   const int64_t nd = (int64_t)t.dn[0] * t.dn[1];
-  for (int s = nsub - 1; s >= 0; --s) {
-    const int n = n0 + s + 1;
-    if (src_h) {
-      tb_sources<true>(t, 1, n, ri0, rj0, RI, RJ, sLE, sLX, sLY);
+  // as in k_tmz_tb_fwd: a copy of the loop without the CPML path for
+  // regions that have no CPML point inside a profile
+  const bool psi_any = __syncthreads_or(any & (kTmzPsiE | kTmzPsiX | kTmzPsiY)) != 0;
+  auto steps = [&](auto tag) {
+    constexpr bool PSI = decltype(tag)::value;
+    for (int s = nsub - 1; s >= 0; --s) {
+      const int n = n0 + s + 1;
+      if (src_h) {
+        tb_sources<true>(t, 1, n, ri0, rj0, RI, RJ, sLE, sLX, sLY);
+        __syncthreads();
+      }
+      // H half: the curl weight of every Hx / Hy point, then lambda_E gathers
+  #pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int k = (ty + kTbRows * q) * RJ + c;
+        sW1[k] = (fl[q] & kTmzPlainX) ? pt[q].cxn * sLX[k]
+                 : (PSI && (fl[q] & kTmzPsiX))
+                     ? adjx_cpml<P, true>(g, fl[q], pt[q].cxn, j, sLX[k], sP + 2 * NP + k,
+                                          sP + 2 * NP + k)
+                     : 0.f;
+        sW2[k] = (fl[q] & kTmzPlainY) ? pt[q].cy * sLY[k]
+                 : (PSI && (fl[q] & kTmzPsiY))
+                     ? adjy_cpml<P, true>(g, fl[q], pt[q].cy, li[q], sLY[k], sP + 3 * NP + k,
+                                          sP + 3 * NP + k)
+                     : 0.f;
+      }
       __syncthreads();
-    }
-    // H half: the curl weight of every Hx / Hy point, then lambda_E gathers
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int k = (ty + kTbRows * q) * RJ + c;
-      sW1[k] = (fl[q] & kTmzPlainX) ? pt[q].cxn * sLX[k]
-               : (fl[q] & kTmzPsiX)
-                   ? adjx_cpml<P, true>(g, fl[q], pt[q].cxn, j, sLX[k], sP + 2 * NP + k,
-                                        sP + 2 * NP + k)
-                   : 0.f;
-      sW2[k] = (fl[q] & kTmzPlainY) ? pt[q].cy * sLY[k]
-               : (fl[q] & kTmzPsiY)
-                   ? adjy_cpml<P, true>(g, fl[q], pt[q].cy, li[q], sLY[k], sP + 3 * NP + k,
-                                        sP + 3 * NP + k)
-                   : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int a = ty + kTbRows * q, k = a * RJ + c;
-      if (a >= 1 && c >= 1) {
-        float le = sLE[k];
-        if (fl[q] & kTmzMonitor) {
-          bool has;
-          le = le + P::from_double(seed_of(g, t, b, li[q], j, n, &has));
+  #pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int a = ty + kTbRows * q, k = a * RJ + c;
+        if (a >= 1 && c >= 1) {
+          float le = sLE[k];
+          if (fl[q] & kTmzMonitor) {
+            bool has;
+            le = le + P::from_double(seed_of(g, t, b, li[q], j, n, &has));
+          }
+          sLE[k] = le + ((sW1[k - 1] - sW1[k]) + (sW2[k - RJ] - sW2[k]));
         }
-        sLE[k] = le + ((sW1[k - 1] - sW1[k]) + (sW2[k - RJ] - sW2[k]));
       }
-    }
-    __syncthreads();
-    if (src_e) {
-      tb_sources<true>(t, 0, n, ri0, rj0, RI, RJ, sLE, sLX, sLY);
+      __syncthreads();
+      if (src_e) {
+        tb_sources<true>(t, 0, n, ri0, rj0, RI, RJ, sLE, sLX, sLY);
+        __syncthreads();
+      }
+      // E half: the curl weights of every Ez point (and the gradient on tile
+      // design pixels), then lambda_X / lambda_Y gather them
+  #pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int k = (ty + kTbRows * q) * RJ + c;
+        float w1, w2;
+        if (fl[q] & kTmzPlainE) {
+          const float le = sLE[k];
+          w1 = pt[q].c1 * le;
+          w2 = pt[q].c2n * le;
+        } else {
+          w1 = w2 = 0.f;
+          if (PSI && (fl[q] & kTmzPsiE))
+            adje_cpml<P, true, true, true>(g, fl[q], pt[q].c1, li[q], j, sLE[k], sP + k, sP + k,
+                                           sP + NP + k, sP + NP + k, w1, w2);
+        }
+        sW1[k] = w1;
+        sW2[k] = w2;
+        if ((fl[q] & kTmzDesign) && (fl[q] >> 31)) {
+          const int64_t kk = (int64_t)b * nd + design_index(t, li[q], j);
+          const double le = (double)sLE[k];
+          const double inc = (double)static_cast<const float*>(
+              t.hist)[((int64_t)(n - step0 - 1) * t.nb + b) * nd + (kk - (int64_t)b * nd)];
+          t.grad[kk] += le * inc * t.dc[kk].neg_reps;
+        }
+      }
+      __syncthreads();
+  #pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int a = ty + kTbRows * q, k = a * RJ + c;
+        if (a < RI - 1 && c < RJ - 1) {
+          sLX[k] = sLX[k] + (sW2[k] - sW2[k + 1]);
+          sLY[k] = sLY[k] + (sW1[k] - sW1[k + RJ]);
+        }
+      }
       __syncthreads();
     }
-    // E half: the curl weights of every Ez point (and the gradient on tile
-    // design pixels), then lambda_X / lambda_Y gather them
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int k = (ty + kTbRows * q) * RJ + c;
-      float w1, w2;
-      if (fl[q] & kTmzPlainE) {
-        const float le = sLE[k];
-        w1 = pt[q].c1 * le;
-        w2 = pt[q].c2n * le;
-      } else {
-        w1 = w2 = 0.f;
-        if (fl[q] & kTmzPsiE)
-          adje_cpml<P, true, true, true>(g, fl[q], pt[q].c1, li[q], j, sLE[k], sP + k, sP + k,
-                                         sP + NP + k, sP + NP + k, w1, w2);
-      }
-      sW1[k] = w1;
-      sW2[k] = w2;
-      if ((fl[q] & kTmzDesign) && (fl[q] >> 31)) {
-        const int64_t kk = (int64_t)b * nd + design_index(t, li[q], j);
-        const double le = (double)sLE[k];
-        const double inc = (double)static_cast<const float*>(
-            t.hist)[((int64_t)(n - step0 - 1) * t.nb + b) * nd + (kk - (int64_t)b * nd)];
-        t.grad[kk] += le * inc * t.dc[kk].neg_reps;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int a = ty + kTbRows * q, k = a * RJ + c;
-      if (a < RI - 1 && c < RJ - 1) {
-        sLX[k] = sLX[k] + (sW2[k] - sW2[k + 1]);
-        sLY[k] = sLY[k] + (sW1[k] - sW1[k + RJ]);
-      }
-    }
-    __syncthreads();
-  }
+  };
+  if (psi_any)
+    steps(PsiTag<true>{});
+  else
+    steps(PsiTag<false>{});
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     if (!(fl[q] >> 31)) continue;
