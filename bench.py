@@ -492,6 +492,7 @@ def run_serving(args):
         "one_at_a_time": {"value": round(base["gcells_per_s"], 4), "wall_s": round(base["wall_s"], 3)},
         "speedup_vs_one_at_a_time": round(rep["gcells_per_s"] / base["gcells_per_s"], 3),
         "autotune": tuner.summary(), "clocks": clocks,
+        "gpu_launches": rep["launches"],
     }
     print(json.dumps(result), flush=True)
 

@@ -97,18 +97,26 @@ class Batch:
             ev.record(self.stream)
             self._staged.append(ev)
 
+    @property
+    def launches_per_step(self):
+        """Kernel launches of one batched step: per half-step the ghost copy
+        (when a grid has ghost planes), the cell update and the sources (when
+        a grid has any)."""
+        return 2 * (int(self.b.ghosts > 0) + 1 + int(self.b.srcs > 0))
+
     def run(self, steps, n0s=None):
         """Advance grid i by steps[i] steps (one chunk; max(steps) <= every src_chunk).
 
         ``n0s[i]`` is grid i's current time step (for its source values).
         Work is enqueued on ``self.stream``; call ``synchronize()`` to wait.
+        Returns the number of kernels it launched.
         """
         steps = [int(s) for s in steps]
         if len(steps) != len(self.engines):
             raise ValueError("one step count per grid")
         k = max(steps) if steps else 0
         if k == 0:
-            return
+            return 0
         self.stage(steps, n0s if n0s is not None else [0.0] * len(steps))
         for i, s in enumerate(steps):
             self._steps[i] = s
@@ -120,6 +128,7 @@ class Batch:
         else:
             N.check(self.lib.gmes_batch_step(C.byref(self.b), k, self.blocks,
                                              C.c_void_p(self.stream.cuda_stream)))
+        return k * self.launches_per_step
 
     def synchronize(self):
         self.stream.synchronize()

@@ -88,6 +88,7 @@ class Server:
         self._batch = None
         self._batch_key = None
         self.chunks = 0
+        self.launches = 0
 
     # -- admission ---------------------------------------------------------
     @staticmethod
@@ -208,7 +209,7 @@ class Server:
             n0s = [float(j.done) for j in self.resident]
             if self.tuner is not None:
                 self.tuner.observe_start(batch)
-            batch.run(steps, n0s)
+            self.launches += batch.run(steps, n0s)
             # host work overlaps the chunk: compile the next arrivals' scenes
             for job in waiting[:4]:
                 self._compile(job)
@@ -238,7 +239,7 @@ class Server:
             "gcells_per_s": cell_updates / wall / 1e9 if wall > 0 else 0.0,
             "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
-            "chunks": self.chunks,
+            "chunks": self.chunks, "launches": self.launches,
         }
 
 
