@@ -36,10 +36,11 @@ def air2d(precision="fp64", verbose=False):
 
 
 def cube(n=256, nobj=24, seed=0, pml_cells=10, precision="fp64", verbose=False, res=10,
-         src_time=None):
+         src_time=None, kappa_max=1.0):
     """The 3-D dielectric + CPML benchmark scene on an n^3 grid (resolution 10).
 
-    ``src_time`` replaces the Bandpass(0.5, 0.2) pulse (peak at t = 50).
+    ``src_time`` replaces the Bandpass(0.5, 0.2) pulse (peak at t = 50);
+    ``kappa_max`` is the CPML's kappa grading maximum (1: the default CPML).
     """
     rng = np.random.default_rng(seed)
     dx = 1.0 / res
@@ -56,7 +57,7 @@ def cube(n=256, nobj=24, seed=0, pml_cells=10, precision="fp64", verbose=False, 
         else:
             geom.append(Block(material=Dielectric(eps_inf=eps), center=center,
                               size=(2 * r, 2 * r, 2 * r)))
-    geom.append(Shell(material=Cpml(), thickness=pml_cells * dx))
+    geom.append(Shell(material=Cpml(kappa_max=kappa_max), thickness=pml_cells * dx))
     src = [PointSource(src_time=src_time or Bandpass(freq=0.5, fwidth=0.2), center=(0, 0, 0),
                        component=Ex)]
     space = Cartesian(size=(size, size, size), resolution=res)

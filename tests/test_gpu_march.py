@@ -45,6 +45,9 @@ BUILDERS = {
     "cube45": (lambda p: W.cube(n=45, nobj=6, pml_cells=5, precision=p, src_time=PULSE), 120),
     "disp40": (lambda p: W.dispersive(n=40, pml_cells=6, precision=p, res=10, src_time=PULSE),
                120),
+    # kappa > 1 inside the slabs, kappa == 1 at their inner edge: both CPML forms
+    "cube45_kappa4": (lambda p: W.cube(n=45, nobj=6, pml_cells=5, precision=p, src_time=PULSE,
+                                       kappa_max=4.0), 120),
 }
 
 _ref = {}
