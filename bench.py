@@ -156,31 +156,35 @@ def measured_peak():
     return 6800.0, "of fallback"
 
 
-def ncu_traffic(workload_key, precision):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "traffic.json"
+def _profile_entry(name, workload_key, precision, side):
+    """An entry of a committed ncu summary: the H half-step's own entry
+    (key suffix /H) when the H half is the dominant kernel and has one,
+    else the workload's entry (the E half-step)."""
+    p = ROOT / "profiles" / name
     if not p.exists():
         return None
     try:
         data = json.loads(p.read_text())
-        return data.get(f"{workload_key}/{precision}")
     except ValueError:
         return None
+    key = f"{workload_key}/{precision}"
+    if side == "H" and f"{key}/H" in data:
+        return data[f"{key}/H"]
+    return data.get(key)
 
 
-def ncu_pipe(workload_key, precision):
+def ncu_traffic(workload_key, precision, side="E"):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    return _profile_entry("traffic.json", workload_key, precision, side)
+
+
+def ncu_pipe(workload_key, precision, side="E"):
     """The busiest execution pipe of the dominant kernel (committed ncu summary).
 
     Where a kernel is bound by an arithmetic pipe rather than by DRAM (the
     FP64 cell kernel: FP64 pipe), this says which pipe and how busy it was.
     """
-    p = ROOT / "profiles" / "pipes.json"
-    if not p.exists():
-        return None
-    try:
-        return json.loads(p.read_text()).get(f"{workload_key}/{precision}")
-    except ValueError:
-        return None
+    return _profile_entry("pipes.json", workload_key, precision, side)
 
 
 # ---------------------------------------------------------------------------
@@ -360,7 +364,8 @@ def run_ours(args):
     peak, peak_src = measured_peak()
     achieved = dom[1] / (dom[2] / 1e3) / 1e9
     step_bytes = eb + hb
-    traffic = ncu_traffic(cfg["workload"], args.precision)
+    side = dom[0][0]
+    traffic = ncu_traffic(cfg["workload"], args.precision, side)
     result = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5),
@@ -376,7 +381,7 @@ def run_ours(args):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": dom[0], "alg_bytes_per_launch": dom[1],
                      "launch_ms": round(dom[2], 5), "peak_source": peak_src,
-                     "pipe": ncu_pipe(cfg["workload"], args.precision)},
+                     "pipe": ncu_pipe(cfg["workload"], args.precision, side)},
         "half_ms": {"E": round(e_ms, 5), "H": round(h_ms, 5)},
         "gpu_launches": args.steps * (6 if scene.sources else 4),
         "clocks": clocks,

@@ -111,13 +111,19 @@ __device__ __forceinline__ bool kappa_one(const Coef* q) {
 // share the first two FMAs, and a psi block runs only in warps where some
 // lane is inside that axis' slab.  The separate CPML form ran both forms in
 // every warp that straddles a slab edge along the contiguous axis.  Points
-// with kappa != 1 take the separate form.  Measured on GB300 (256^3 cube,
-// 10-cell CPML), FP64: 17.6 -> 16.8 FP64 warp-instructions per cell,
-// 14.23 -> 14.93 Gcell/s.  FP32 runs slower with it (32.9 -> 31.2) and the
-// float-float type has no psi votes, so both keep the separate form.  The
-// same form with the psi updates predicated inside the votes, or with a
-// kappa correction term in the shared path, issued more FP64 instructions
-// (19.0 and 24.1 per cell).
+// with kappa != 1 take the separate form.  A __syncwarp at the top of each
+// voted psi block keeps it a branch: without it the compiler predicated
+// the blocks and every warp with a CPML lane issued both.  Measured on
+// GB300 (256^3 cube, 10-cell CPML), FP64 warp-instructions per cell and
+// half-step (E side) and Gcell/s:
+//   separate form, psi votes                 17.6   14.23
+//   shared form, votes                       16.8   14.93
+//   shared form, votes + __syncwarp          14.4   16.17
+// 14.4 is what a warp-level count of the slabs predicts when each psi block
+// issues only in warps that need it.  FP32 (32.7 -> 30.7 Gcell/s) and the
+// float-float type (19.6 -> 18.5) run slower with the shared form, and
+// slower with __syncwarp in their own psi votes, so both keep the
+// separate form.
 template <class P>
 struct SharedCpml {
   static constexpr bool value = false;
@@ -164,6 +170,7 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
           T* aux = static_cast<T*>(g.aux[C]);
           const R cdt = P::cfg(&cc.cdt);
           if (__any_sync(am, on1)) {
+            __syncwarp(am);  // keeps the block a branch
             const R n1 = P::cfg(q1) * pre.a + P::cfg(q1 + 3) * p1;
             if (on1) {
               P::st(aux + lin, n1);
@@ -171,6 +178,7 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
             }
           }
           if (__any_sync(am, on2)) {
+            __syncwarp(am);  // keeps the block a branch
             const R n2 = P::cfg(q2) * pre.b + P::cfg(q2 + 3) * p2;
             if (on2) {
               P::st(aux + g.npts[C] + lin, n2);
