@@ -30,8 +30,8 @@ constexpr int kThreads = 256;
 // Measured on GB300 (256^3 cube): FP32 runs 8% faster at 5 blocks (48
 // registers) than at 4 (56); 6 and 8 blocks spill and run slower.  FP64
 // and df64 run best at 4 (64 registers): at 5 they spill and lose 5% and
-// 12%, at 3 FP64 loses 3%.  GMES_MIN_BLOCKS overrides every precision
-// (tuning builds).
+// 12%, at 3 (74-80 registers, no spills) FP64 loses 13% (16.17 -> 14.13
+// Gcell/s).  GMES_MIN_BLOCKS overrides every precision (tuning builds).
 #ifdef GMES_MIN_BLOCKS
 template <class P>
 struct MinBlocks {
