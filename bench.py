@@ -283,13 +283,15 @@ def e2e_loop(sim, steps):
     idx = src.idx if src else (0, 0, 0)
     field = sim.engine.fields[c]
     probe = torch.empty((1,) + tuple(field.shape[3:]), dtype=field.dtype).pin_memory()
+    # a view of the probed point, made once: each step copies its current value
+    point = field[idx].reshape(probe.shape)
     for _ in range(3):
         sim.step()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
         sim.step()
-        probe.copy_(field[idx].reshape(probe.shape), non_blocking=True)
+        probe.copy_(point, non_blocking=True)
         torch.cuda.current_stream().synchronize()
     wall = time.perf_counter() - t0
     h2d = 2 * len(scene.sources) * 8

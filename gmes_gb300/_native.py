@@ -34,6 +34,7 @@ EXPORTS = [
     "gmes_graph_destroy", "gmes_rasterize", "gmes_batch_step_noalloc",
     "gmes_tmz_sizes", "gmes_tmz_check", "gmes_tmz_set_design", "gmes_tmz_reset",
     "gmes_tmz_forward", "gmes_tmz_objective", "gmes_tmz_adjoint", "gmes_points_update",
+    "gmes_copy_async",
 ]
 NOALLOC_MAX_GRIDS = 64
 
@@ -180,6 +181,7 @@ def load():
     lib.gmes_rasterize.argtypes = [P(GridDescC), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                    C.c_void_p]
     lib.gmes_graph_destroy.argtypes = [C.c_void_p]
+    lib.gmes_copy_async.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     G, B = P(GridDescC), P(TmzBatchC)
     lib.gmes_tmz_sizes.argtypes = [G, B, P(C.c_int64)]
     lib.gmes_tmz_check.argtypes = [G, B]

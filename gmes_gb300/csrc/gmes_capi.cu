@@ -649,6 +649,16 @@ gmes_status gmes_graph_destroy(void* graph_exec) {
   return GMES_OK;
 }
 
+gmes_status gmes_copy_async(void* dst, const void* src, int64_t bytes, void* stream) {
+  if (bytes < 0) return fail(GMES_ERR_VALUE, "negative copy size");
+  if (bytes == 0) return GMES_OK;
+  if (dst == nullptr || src == nullptr) return fail(GMES_ERR_VALUE, "copy pointer is NULL");
+  cudaError_t e = cudaMemcpyAsync(dst, src, static_cast<size_t>(bytes), cudaMemcpyDefault,
+                                  static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "copying");
+  return GMES_OK;
+}
+
 gmes_status gmes_rasterize(const gmes_grid_desc* g, int32_t comp, const gmes_shape* shapes,
                            int32_t nshapes, const uint8_t* lut, void* stream) {
   gmes_status st = check_desc(g, true);

@@ -120,10 +120,11 @@ class GridEngine:
             self.src_val = torch.zeros(lead + (self.src_chunk, 2, len(srcs)), dtype=torch.float64,
                                        device=dev)
             self.src_host = torch.zeros(self.src_val.shape, dtype=torch.float64).pin_memory()
+            self._src_host_np = self.src_host.numpy()  # shares the pinned memory
             d.src = self.src.data_ptr()
             d.src_val = self.src_val.data_ptr()
         else:
-            self.src = self.src_val = self.src_host = None
+            self.src = self.src_val = self.src_host = self._src_host_np = None
         # TFSF: the incident-field grid (advanced inside this grid's step) and
         # the transparent points
         self.incident = None
@@ -145,7 +146,12 @@ class GridEngine:
         self.probes = None
         self.probe_val = None
         self.desc = d
-        self._staged = None
+        # events reused on every call: the pinned staging buffer's last copy,
+        # and the two directions of ordering against the caller's stream
+        self._staged = torch.cuda.Event()
+        self._ev_in = torch.cuda.Event()
+        self._ev_out = torch.cuda.Event()
+        self._dev_index = dev.index if dev.index is not None else torch.cuda.current_device()
         self._rows, self._pool, self._pmls = rows, pool, pmls
         # The engine works on its own (non-default) stream so that chunks of
         # steps can be captured as CUDA graphs; it orders itself against the
@@ -179,14 +185,16 @@ class GridEngine:
         return self._stream
 
     def _enter(self):
-        cur = _torch().cuda.current_stream(self.device)
+        cur = _torch().cuda.current_stream(self._dev_index)
         if cur.cuda_stream != self._stream.cuda_stream:
-            self._stream.wait_stream(cur)
+            self._ev_in.record(cur)
+            self._stream.wait_event(self._ev_in)
 
     def _leave(self):
-        cur = _torch().cuda.current_stream(self.device)
+        cur = _torch().cuda.current_stream(self._dev_index)
         if cur.cuda_stream != self._stream.cuda_stream:
-            cur.wait_stream(self._stream)
+            self._ev_out.record(self._stream)
+            cur.wait_event(self._ev_out)
 
     # -- setup -------------------------------------------------------------
     def build_coefficients(self):
@@ -330,25 +338,26 @@ class GridEngine:
             N.check(self.lib.gmes_step(C.byref(self.desc), int(nsteps), C.c_void_p(self.stream)))
 
     def _stage(self, vals, k, stream=None):
-        torch = _torch()
         stream = stream if stream is not None else self._stream
         # the pinned staging buffer may still be read by the previous
         # chunk's asynchronous copy
-        if self._staged is not None:
-            self._staged.synchronize()
+        self._staged.synchronize()
         vals = np.asarray(vals)
+        host = self._src_host_np
         if self.cmplx:
-            self.src_host[0, :k].copy_(torch.from_numpy(np.ascontiguousarray(vals.real)))
-            self.src_host[1, :k].copy_(torch.from_numpy(np.ascontiguousarray(vals.imag)))
+            host[0, :k] = vals.real
+            host[1, :k] = vals.imag
         else:
-            self.src_host[:k].copy_(torch.from_numpy(np.ascontiguousarray(vals)))
-        with torch.cuda.stream(stream):
-            if self.cmplx:
-                self.src_val[:, :k].copy_(self.src_host[:, :k], non_blocking=True)
-            else:
-                self.src_val[:k].copy_(self.src_host[:k], non_blocking=True)
-            self._staged = torch.cuda.Event()
-            self._staged.record(stream)
+            host[:k] = vals
+        # rows of (2, nsrc) float64 per step; a complex grid has a real and
+        # an imaginary plane of src_chunk rows each
+        row = host.shape[-1] * host.shape[-2] * 8
+        plane = self.src_chunk * row
+        for q in range(2 if self.cmplx else 1):
+            N.check(self.lib.gmes_copy_async(C.c_void_p(self.src_val.data_ptr() + q * plane),
+                                             C.c_void_p(self.src_host.data_ptr() + q * plane),
+                                             k * row, C.c_void_p(stream.cuda_stream)))
+        self._staged.record(stream)
 
     def _stage_incident(self, n0, k):
         """Stage the incident-field grid's source values on this grid's stream."""

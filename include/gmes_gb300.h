@@ -380,6 +380,16 @@ gmes_status gmes_graph_launch(void* graph_exec, void* stream);
 gmes_status gmes_graph_destroy(void* graph_exec);
 
 /*
+ * Asynchronous copy of `bytes` bytes between host and device memory on
+ * `stream` (direction from the pointers; pinned host memory makes it truly
+ * asynchronous).  Used to stage a chunk's source values ahead of its launch
+ * (the per-step host inputs of gmes/pw_source.py:80) without a runtime call
+ * from the host language.  bytes == 0 is a no-op; a negative size or a NULL
+ * pointer with bytes > 0 is GMES_ERR_VALUE.
+ */
+gmes_status gmes_copy_async(void* dst, const void* src, int64_t bytes, void* stream);
+
+/*
  * Material-map builder on the GPU (replaces the per-point Python loop of
  * FDTD.init_material_*, gmes/fdtd.py:353-477, and the geometry tree lookups
  * of src/pygeom.pyx:300-454).  Every point of component `comp` takes the

@@ -153,3 +153,15 @@ def test_tmz_sizes_and_validation():
     d.precision = N.FP64_STRICT
     with pytest.raises(ValueError):
         N.check(lib.gmes_tmz_sizes(C.byref(d), C.byref(_tmz()), sizes))
+
+
+def test_copy_async_validates_before_any_copy():
+    lib = N.load()
+    buf = (C.c_char * 16)()
+    ok, err_value = 0, 1  # GMES_OK, GMES_ERR_VALUE
+    assert lib.gmes_copy_async(None, None, 0, None) == ok  # nothing to copy
+    assert lib.gmes_copy_async(buf, buf, -1, None) == err_value
+    assert b"negative" in lib.gmes_last_error()
+    assert lib.gmes_copy_async(None, buf, 8, None) == err_value
+    assert lib.gmes_copy_async(buf, None, 8, None) == err_value
+    assert b"NULL" in lib.gmes_last_error()
