@@ -517,7 +517,7 @@ gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs
     return fail(GMES_ERR_VALUE, "NULL argument");
   if (njobs < 1) return fail(GMES_ERR_VALUE, "njobs = %d must be >= 1", njobs);
   if (bx_cap < 0 || bx_cap > 5) return fail(GMES_ERR_VALUE, "bx_cap = %d outside [0, 5]", bx_cap);
-  if (bx_cap == 0) bx_cap = 5;
+  if (bx_cap == 0) bx_cap = 4;  // 16-cell rows, as the single-grid kernel
   const BatchLayout L = batch_layout(njobs);
   if (workspace_bytes < L.total)
     return fail(GMES_ERR_VALUE, "workspace of %lld bytes, %lld needed",
@@ -1058,7 +1058,7 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
                 njobs, GMES_NOALLOC_MAX_GRIDS);
   if (nsteps < 0) return fail(GMES_ERR_VALUE, "nsteps = %d must be >= 0", nsteps);
   if (bx_cap < 0 || bx_cap > 5) return fail(GMES_ERR_VALUE, "bx_cap = %d outside [0, 5]", bx_cap);
-  if (bx_cap == 0) bx_cap = 5;
+  if (bx_cap == 0) bx_cap = 4;  // 16-cell rows, as the single-grid kernel
   const BatchLayout L = batch_layout(njobs);
   if (L.total > kNoAllocBytes)
     return fail(GMES_ERR_RUNTIME, "batch tables of %lld bytes exceed the fixed %lld",

@@ -656,6 +656,21 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<P>::value)
   cell_body<P, SIDE, STRICT, DISP, MASK, I>(g, i, j, k);
 }
 
+// Cells per block row along k (log2): a warp covers 16 cells of two rows
+// (128 bytes per row in FP64 and df64, 64 in FP32).  Against 32 cells of
+// one row, a warp straddles a material or CPML edge along k in half as many
+// places, so fewer warps run two kinds' code or a psi block for a few
+// lanes.  Measured on GB300, Gcell/s, rows of 32 / 16 / 8 cells:
+//   256^3 cube (dielectric + CPML)   FP64 16.17 / 16.81 / 15.99
+//                                    FP32 32.99 / 33.74 / 29.36
+//                                    df64 19.72 / 21.12 / 20.12
+//   192^3 dispersive + UPML          FP64  8.06 /  9.42 /  9.69
+//                                    FP32 19.34 / 20.08 / 18.47
+//                                    df64 12.73 / 13.86 / 13.80
+// (FP64 E half of the cube: 14.4 -> 13.7 FP64 warp-instructions per cell,
+// what a warp-level count of the slabs predicts for both shapes.)
+constexpr int kRowLog2 = 4;
+
 template <class P, bool STRICT, int MASK, class I>
 void launch_cell(const GridDev& d, int side, bool disp, dim3 grid, int bx_log2, int i0,
                  cudaStream_t s) {
@@ -970,7 +985,7 @@ void run_half(const Plan& p, int side, int st, cudaStream_t s) {
   else
     k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
   int bx_log2 = 0;
-  while (bx_log2 < 5 && (1 << bx_log2) < d.n[2]) ++bx_log2;
+  while (bx_log2 < kRowLog2 && (1 << bx_log2) < d.n[2]) ++bx_log2;
   const int bx = 1 << bx_log2, by = kThreads / bx;
   const int nplanes = p.cplx ? 2 : 1;
   for (int part = 0; part < nplanes; ++part) {

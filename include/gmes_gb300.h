@@ -318,7 +318,7 @@ typedef struct {
 
 int64_t gmes_batch_workspace_size(int32_t njobs);
 
-/* bx_cap: log2 of the largest block extent along k (0..5; 0 = default 5). */
+/* bx_cap: log2 of the largest block extent along k (0..5; 0 = default 4). */
 gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs,
                                void* workspace, int64_t workspace_bytes, int32_t bx_cap,
                                gmes_batch* out, void* stream);
