@@ -2,10 +2,14 @@
 
 A ``Batch`` holds a set of ``GridEngine`` objects of one precision.  Each
 chunk of steps runs as ONE launch per kernel kind per half-step for the
-whole batch (``gmes_batch_step``), captured as a CUDA graph per chunk
-length.  Each grid takes its own number of steps in a chunk, so grids of
-different sizes and step counts share the device without waiting for one
-another; a grid's arithmetic is the same as when it runs alone.
+small grids of the batch (``gmes_batch_step``), captured as a CUDA graph
+per chunk length; grids of ``solo_cells`` cells or more fill the GPU on
+their own and run their single-grid kernels (their own chunk graph) on the
+batch's stream, where the multi-grid kernel's per-block job look-up and
+descriptor loads would only slow them.  Each grid takes its own number of
+steps in a chunk, so grids of different sizes and step counts share the
+device without waiting for one another; a grid's arithmetic is the same as
+when it runs alone.
 """
 
 import ctypes as C
@@ -17,15 +21,25 @@ from .engine import _torch
 from .scene import source_values
 
 
+# Grids of at least this many cells run their own single-grid kernels in a
+# batch.  Measured on GB300 (64-job FP64 serving mix, 2-D 128^2-1024^2 and
+# 3-D 64^3-160^3): the multi-grid kernel alone ran the mix at 8.47 Gcell/s
+# against 8.74 one grid at a time.
+SOLO_CELLS = 1 << 20
+
+
 class Batch:
     """A fixed set of grids stepped together.
 
     ``bx_cap`` (0..5) caps the block's extent along k at 2**bx_cap;
     ``blocks`` is the grid size of the persistent update kernel (0: one
     block per tile).  Both are launch-shape knobs the autotuner sets.
+    ``solo_cells``: grids with at least this many cells run their own
+    single-grid kernels (0: every grid through the multi-grid kernel).
     """
 
-    def __init__(self, engines, bx_cap=0, blocks=0, use_graphs=True, stream=None):
+    def __init__(self, engines, bx_cap=0, blocks=0, use_graphs=True, stream=None,
+                 solo_cells=SOLO_CELLS):
         torch = _torch()
         if not engines:
             raise ValueError("a batch needs at least one grid")
@@ -40,20 +54,37 @@ class Batch:
         self.bx_cap = int(bx_cap)
         self.use_graphs = bool(use_graphs)
         self._graphs = {}
-        n = len(self.engines)
-        ws = int(self.lib.gmes_batch_workspace_size(n))
-        self.workspace = torch.empty(ws, dtype=torch.uint8, device=self.device)
-        # descriptors must outlive the batch: they are referenced by pointer
-        self._descs = (C.POINTER(N.GridDescC) * n)(*[C.pointer(e.desc) for e in self.engines])
-        self.b = N.BatchC()
+        solo_cells = int(solo_cells)
+        self.solo = [i for i, e in enumerate(self.engines)
+                     if solo_cells > 0 and e.scene.cells >= solo_cells]
+        self.multi = [i for i in range(len(self.engines)) if i not in self.solo]
+        for i in self.solo:
+            # the multi-grid kernel's conditions, so that a grid is batchable
+            # or not whatever its size
+            d = self.engines[i].desc
+            if d.ntfsf > 0:
+                raise ValueError(f"grid {i} has a TFSF source: not batchable")
+            if d.nprobe > 0:
+                raise ValueError(f"grid {i} has probes: not batchable")
+            if self.engines[i].cmplx:
+                raise ValueError(f"grid {i} is complex: not batchable")
         cur = torch.cuda.current_stream(self.device)
         self.stream.wait_stream(cur)
         for e in self.engines:
             self.stream.wait_stream(e.torch_stream)
-        N.check(self.lib.gmes_batch_prepare(self._descs, n, C.c_void_p(self.workspace.data_ptr()),
-                                            ws, self.bx_cap, C.byref(self.b),
-                                            C.c_void_p(self.stream.cuda_stream)))
-        self._steps = (C.c_int32 * n)()
+        self.b = None
+        n = len(self.multi)
+        if n:
+            ws = int(self.lib.gmes_batch_workspace_size(n))
+            self.workspace = torch.empty(ws, dtype=torch.uint8, device=self.device)
+            # descriptors must outlive the batch: they are referenced by pointer
+            self._descs = (C.POINTER(N.GridDescC) * n)(
+                *[C.pointer(self.engines[i].desc) for i in self.multi])
+            self.b = N.BatchC()
+            N.check(self.lib.gmes_batch_prepare(
+                self._descs, n, C.c_void_p(self.workspace.data_ptr()), ws, self.bx_cap,
+                C.byref(self.b), C.c_void_p(self.stream.cuda_stream)))
+            self._steps = (C.c_int32 * n)()
         self._staged = []
 
     def __del__(self):
@@ -65,7 +96,8 @@ class Batch:
 
     @property
     def tiles(self):
-        return int(self.b.tiles)
+        """Tiles of the multi-grid kernel (0 when every grid runs solo)."""
+        return int(self.b.tiles) if self.b is not None else 0
 
     def _graph(self, nsteps):
         key = (nsteps, self.blocks)
@@ -97,12 +129,24 @@ class Batch:
             ev.record(self.stream)
             self._staged.append(ev)
 
+    def _multi_launches_per_step(self):
+        """Launches of one multi-grid step: per half-step the ghost copy (when
+        a grid has ghost planes), the cell update and the sources (when a grid
+        has any)."""
+        if self.b is None:
+            return 0
+        return 2 * (int(self.b.ghosts > 0) + 1 + int(self.b.srcs > 0))
+
+    def _solo_launches_per_step(self, i):
+        """Launches of one single-grid step: per half-step the ghost copy, the
+        cell update and the sources (when the grid has any)."""
+        return 2 * (2 + int(self.engines[i].desc.nsrc > 0))
+
     @property
     def launches_per_step(self):
-        """Kernel launches of one batched step: per half-step the ghost copy
-        (when a grid has ghost planes), the cell update and the sources (when
-        a grid has any)."""
-        return 2 * (int(self.b.ghosts > 0) + 1 + int(self.b.srcs > 0))
+        """Kernel launches of one step of every grid of the batch."""
+        return self._multi_launches_per_step() + sum(self._solo_launches_per_step(i)
+                                                     for i in self.solo)
 
     def run(self, steps, n0s=None):
         """Advance grid i by steps[i] steps (one chunk; max(steps) <= every src_chunk).
@@ -118,17 +162,31 @@ class Batch:
         if k == 0:
             return 0
         self.stage(steps, n0s if n0s is not None else [0.0] * len(steps))
-        for i, s in enumerate(steps):
-            self._steps[i] = s
-        N.check(self.lib.gmes_batch_set_steps(C.byref(self.b), self._steps,
-                                              C.c_void_p(self.stream.cuda_stream)))
-        if self.use_graphs:
-            N.check(self.lib.gmes_graph_launch(C.c_void_p(self._graph(k)),
-                                               C.c_void_p(self.stream.cuda_stream)))
-        else:
-            N.check(self.lib.gmes_batch_step(C.byref(self.b), k, self.blocks,
-                                             C.c_void_p(self.stream.cuda_stream)))
-        return k * self.launches_per_step
+        st = C.c_void_p(self.stream.cuda_stream)
+        launched = 0
+        km = max((steps[i] for i in self.multi), default=0)
+        if km > 0:
+            for q, i in enumerate(self.multi):
+                self._steps[q] = steps[i]
+            N.check(self.lib.gmes_batch_set_steps(C.byref(self.b), self._steps, st))
+            if self.use_graphs:
+                N.check(self.lib.gmes_graph_launch(C.c_void_p(self._graph(km)), st))
+            else:
+                N.check(self.lib.gmes_batch_step(C.byref(self.b), km, self.blocks, st))
+            launched += km * self._multi_launches_per_step()
+        for i in self.solo:
+            s = steps[i]
+            if s <= 0:
+                continue
+            e = self.engines[i]
+            # the chunk length every grid shares is replayed as the grid's
+            # own graph; a shorter last chunk runs as plain launches
+            if self.use_graphs and s == k:
+                N.check(self.lib.gmes_graph_launch(C.c_void_p(e._graph(s)), st))
+            else:
+                N.check(self.lib.gmes_step(C.byref(e.desc), s, st))
+            launched += s * self._solo_launches_per_step(i)
+        return launched
 
     def synchronize(self):
         self.stream.synchronize()

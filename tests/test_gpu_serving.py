@@ -57,6 +57,30 @@ def test_batch_equals_alone(precision, shape):
             assert np.array_equal(eng.read(c), ref[c]), (precision, shape, c)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "df64", "fp32"])
+@pytest.mark.parametrize("solo_cells", [8000, 1])
+def test_batch_with_solo_grids_equals_alone(precision, solo_cells):
+    """Grids above the size threshold run their single-grid kernels inside the
+    batch (as a graph for a full chunk, as plain launches for a shorter last
+    one); every grid still matches its run alone bit for bit."""
+    jobs = mix()
+    engines = [GridEngine(b().compile(), precision=precision, src_chunk=32) for b, _ in jobs]
+    batch = Batch(engines, solo_cells=solo_cells)
+    assert batch.solo and (solo_cells == 1) == (not batch.multi)
+    done = [0] * len(jobs)
+    launched = 0
+    while any(d < n for d, (_, n) in zip(done, jobs)):
+        steps = [min(32, n - d) for d, (_, n) in zip(done, jobs)]
+        launched += batch.run(steps, [float(d) for d in done])
+        done = [d + s for d, s in zip(done, steps)]
+    batch.synchronize()
+    assert launched > 0
+    for (b, n), eng in zip(jobs, engines):
+        ref = alone(b, n, precision)
+        for c in range(6):
+            assert np.array_equal(eng.read(c), ref[c]), (precision, solo_cells, c)
+
+
 def test_graph_chunks_equal_plain_launches():
     b, n = mix()[3]
     e1 = GridEngine(b().compile(), use_graphs=True, src_chunk=16)
