@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--block-steps", type=int, default=0,
                     help="design2d, fp32: steps per kernel launch (0: temporally blocked "
                          "default, 1: one step per launch)")
+    ap.add_argument("--segment", type=int, default=0,
+                    help="design2d: √N-checkpoint segment length (0: record the history "
+                         "in the forward when it fits, else ceil(sqrt(steps)))")
     ap.add_argument("--jobs", type=int, default=64, help="serving: number of jobs")
     ap.add_argument("--rate", type=float, default=0.0,
                     help="serving: Poisson arrival rate in jobs/s (0: all at t = 0)")
@@ -507,10 +510,14 @@ def run_serving(args):
 def run_design(args):
     """Gradient of the monitor objective for a batch of TMz designs (512^2, 2000 steps).
 
-    One benchmark step = one forward (J of every design, with checkpoints)
-    plus one backward (recompute + adjoint, dJ/deps of every design).
-    value = cell-updates per second counting forward, recomputed and adjoint
-    steps (3 x cells x steps x designs per benchmark step).
+    One benchmark step = one forward (J of every design, keeping what the
+    backward needs) plus one backward (dJ/deps of every design).  The
+    problem records every step's design increments in the forward when they
+    fit in memory (the default here: 2.1 GB in FP32), so the backward is the
+    adjoint sweep alone; with √N checkpoints (``--segment``) the backward
+    also recomputes the forward.  value = cell-updates per second counting
+    every forward, recomputed and adjoint step run (2 or 3 x cells x steps x
+    designs per benchmark step).
     """
     import torch
     from gmes_gb300 import workloads as W
@@ -519,7 +526,8 @@ def run_design(args):
     n = args.n or 512
     space, geom, src, design, monitor, eps, nsteps = W.design2d(n=n, batch=args.batch)
     prob = TMzAdjoint(space, geom, src, design, monitor, nsteps, batch=args.batch,
-                      precision=precision, block_steps=args.block_steps)
+                      precision=precision, block_steps=args.block_steps,
+                      segment=args.segment or None)
     cells = n * n
     x = torch.tensor(eps, dtype=torch.float64, device="cuda")
     for _ in range(max(1, args.warmup)):
@@ -545,14 +553,15 @@ def run_design(args):
     clocks = clk.stop()
     tf, tb = statistics.median(t_fwd), statistics.median(t_bwd)
     per = tf + tb
-    upd = 3 * cells * nsteps * args.batch
+    passes = 2 if prob.keep_history else 3
+    upd = passes * cells * nsteps * args.batch
     es = 4 if precision == "fp32" else 8
     # algorithmic bytes per cell-step: E half reads Ez, Hx, Hy and writes Ez;
     # H half reads Ez, Hx, Hy and writes Hx, Hy (the adjoint halves the same
     # on the adjoint fields): 9 values.  CPML psi and the class maps (shared
     # by the batch, L2-resident) are not counted.
     fwd_gbs = 9 * es * cells * nsteps * args.batch / tf / 1e9
-    bwd_gbs = 2 * 9 * es * cells * nsteps * args.batch / tb / 1e9
+    bwd_gbs = (passes - 1) * 9 * es * cells * nsteps * args.batch / tb / 1e9
     peak = measured_peak()
     spl = (args.block_steps or 4) if precision == "fp32" else 1  # steps per forward launch
     fwd_kernel = (f"forward, k_tmz_tb_fwd ({spl} steps per launch)" if spl > 1
@@ -565,8 +574,14 @@ def run_design(args):
         "data": "synthetic (seeded designs)",
         "config": {"workload": f"design2d_tmz_{n}x{n}_adjoint", "grid": [n, n, 1],
                    "design_points": [64, 64], "monitor_points": [8, 8], "time_steps": nsteps,
-                   "batch": args.batch, "checkpoint_segment": prob.segment,
-                   "checkpoints": (nsteps + prob.segment - 1) // prob.segment,
+                   "batch": args.batch,
+                   "history": ("forward records every step's design increments "
+                               f"({prob.sizes[3] / 1e9:.2f} GB), no backward recompute"
+                               if prob.keep_history else
+                               f"checkpoints every {prob.segment} steps, backward recompute"),
+                   "checkpoint_segment": None if prob.keep_history else prob.segment,
+                   "checkpoints": (0 if prob.keep_history
+                                   else (nsteps + prob.segment - 1) // prob.segment),
                    "precision": precision, "block_steps": args.block_steps,
                    "l2": "state 7 x batch x n^2 x elem > L2 for batch 64 (inputs larger than L2)"},
         "gradients_per_s": round(args.batch / per, 3),
@@ -594,18 +609,33 @@ def run_design(args):
 
 
 def design_launches(prob, precision, block_steps, max_block_steps=4):
-    """Kernel launches of one forward + backward (recompute and adjoint).
+    """Kernel launches of one forward + backward.
 
-    One step per launch: E, E sources, H, H sources per step in each of the
-    three passes.  FP32 temporally blocked (block_steps 0 = the library's
-    most, 4): one launch per block of steps of each checkpoint segment.
+    One step per launch: E, E sources, H, H sources per step of every pass.
+    FP32 temporally blocked (block_steps 0 = the library's most, 4): the
+    forward takes one launch per block of up to that many steps of each
+    call, the adjoint one per odd block of up to that many steps (1 or 3).
+    Passes: forward and adjoint over all steps when the forward records the
+    history; forward, recompute and adjoint per checkpoint segment otherwise.
     """
     nsteps, seg = prob.nsteps, prob.segment
+    calls = [nsteps] if prob.keep_history else [min(seg, nsteps - s0)
+                                                 for s0 in range(0, nsteps, seg)]
+    passes = 2 if prob.keep_history else 3
     per = (block_steps or max_block_steps) if precision == "fp32" else 1
     if per == 1:
-        return 12 * nsteps
-    segs = [min(seg, nsteps - s0) for s0 in range(0, nsteps, seg)]
-    return 3 * sum((k + per - 1) // per for k in segs)
+        return 4 * passes * nsteps
+
+    def adj(k):
+        n = 0
+        while k > 0:
+            m = min(k, per)
+            m -= 1 - m % 2
+            k -= m
+            n += 1
+        return n
+    fwd = sum((k + per - 1) // per for k in calls)
+    return fwd * (passes - 1) + sum(adj(k) for k in calls)
 
 
 def design_cpu_baseline(space, geom, src, design, monitor, eps, prob, n, steps=100):

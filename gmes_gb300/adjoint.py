@@ -8,9 +8,13 @@ sources) for a batch of designs that share one scene:
   design variables (one value per point);
 * ``TMzAdjoint`` -- the batched forward (``forward``), the objective
   ``J_b = dt * sum_{n=1..N} sum_{monitor} Ez_n^2`` and its gradient by the
-  hand-written time-reversed kernels (``backward``), with checkpoints of
-  the full state every ``segment`` steps (default ceil(sqrt(N))) and the
-  steps of each segment recomputed during the backward sweep;
+  hand-written time-reversed kernels (``backward``).  The adjoint needs the
+  forward Ez increments on the design points of every step.  Where the
+  buffer for all N steps fits (the default when it takes at most a quarter
+  of the free device memory), the forward records them and the backward is
+  the adjoint sweep alone; otherwise the forward keeps checkpoints of the
+  full state every ``segment`` steps (default ceil(sqrt(N))) and the
+  backward recomputes each segment's increments before its adjoint steps;
 * ``TMzAdjoint.objective(eps)`` -- the same behind ``torch.autograd``.
 
 All work runs in the CUDA library (include/gmes_gb300.h, gmes_tmz_*);
@@ -86,11 +90,17 @@ class TMzAdjoint:
     ``block_steps``: FP32 steps per kernel launch (0: the most the
     temporally blocked kernels take, 1: one step per launch); every value
     gives bit-identical fields and gradients.
+    ``keep_history``: True records the design increments of all ``nsteps``
+    steps in the forward (nsteps x batch x design points x element bytes)
+    and skips the backward recompute; False uses √N checkpoints; None
+    chooses False when ``segment`` is given, else True when that buffer
+    takes at most a quarter of the free device memory.  Both give
+    bit-identical J and gradients.
     """
 
     def __init__(self, space, geom_list, src_list, design, monitor, nsteps, batch=1,
                  precision="fp32", segment=None, courant_ratio=0.99, dt=None, device=None,
-                 block_steps=0):
+                 block_steps=0, keep_history=None):
         from .fdtd import TMzFDTD
         torch = _torch()
         if precision not in ("fp32", "fp64", "df64"):
@@ -122,9 +132,17 @@ class TMzAdjoint:
             b.monitor_lo[a], b.monitor_n[a] = m0[a], mn[a]
         b.nsrc = len(rows)
         b.total_steps = self.nsteps
-        b.hist_steps = self.segment
         b.block_steps = int(block_steps)
         sizes = (C.c_int64 * 7)()
+        if keep_history is None and segment:
+            keep_history = False  # a segment length asks for checkpoints
+        if keep_history is None:
+            b.hist_steps = self.nsteps
+            N.check(self.lib.gmes_tmz_sizes(C.byref(self.grid.desc), C.byref(b), sizes))
+            free, _ = torch.cuda.mem_get_info(self.device)
+            keep_history = sizes[3] <= free // 4
+        self.keep_history = bool(keep_history)
+        b.hist_steps = self.nsteps if self.keep_history else self.segment
         N.check(self.lib.gmes_tmz_sizes(C.byref(self.grid.desc), C.byref(b), sizes))
         self.sizes = list(sizes)
         dev = self.device
@@ -216,9 +234,26 @@ class TMzAdjoint:
         self.eps.copy_(e)
 
     def forward(self, eps, checkpoints=True):
-        """J (batch,) float64 device tensor for design permittivities eps (batch, n0, n1)."""
+        """J (batch,) float64 device tensor for design permittivities eps (batch, n0, n1).
+
+        ``checkpoints``: keep what the backward needs (the design increments
+        of every step, or the √N checkpoints).
+        """
         self._set_design(eps)
         torch = _torch()
+        if self.keep_history:
+            g = self.grid
+            g._enter()
+            st = C.c_void_p(g.stream)
+            flags = N.TMZ_RECORD_MONITOR | (N.TMZ_RECORD_HIST if checkpoints else 0)
+            self._call("gmes_tmz_set_design", C.c_void_p(self.eps.data_ptr()), st)
+            self._call("gmes_tmz_reset", 1, st)
+            self._call("gmes_tmz_forward", 0, self.nsteps, flags, st)
+            self._call("gmes_tmz_objective", self.nsteps, C.c_void_p(self.J.data_ptr()), st)
+            g._leave()
+            self._version += 1
+            self._have_checkpoints = bool(checkpoints)
+            return self.J.clone()
         if checkpoints and self.checkpoints is None:
             nseg = (self.nsteps + self.segment - 1) // self.segment
             self.checkpoints = torch.empty((nseg, self.state.numel()), dtype=torch.uint8,
@@ -254,7 +289,10 @@ class TMzAdjoint:
         st = C.c_void_p(g.stream)
         with torch.cuda.stream(g.torch_stream):
             self._call("gmes_tmz_reset", 2, st)
-            for seg, s0, k in reversed(list(self._segments())):
+            if self.keep_history:
+                # the forward recorded every step's increments (slot = step - 1)
+                self._call("gmes_tmz_adjoint", 0, self.nsteps, st)
+            for seg, s0, k in ([] if self.keep_history else reversed(list(self._segments()))):
                 self.state.copy_(self.checkpoints[seg, :self.state.numel()])
                 self._call("gmes_tmz_forward", s0, k, N.TMZ_RECORD_HIST, st)
                 self._call("gmes_tmz_adjoint", s0, k, st)

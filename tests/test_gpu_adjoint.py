@@ -31,11 +31,11 @@ def problem(hard=False, batch=1, n=48, nsteps=160, design_px=6, seed=0):
                       background=BACKGROUND)
 
 
-def make(precision="fp64", batch=1, hard=False, segment=None, **kw):
+def make(precision="fp64", batch=1, hard=False, segment=None, keep_history=None, **kw):
     from gmes_gb300.adjoint import TMzAdjoint
     space, geom, src, design, monitor, eps, nsteps = problem(hard=hard, batch=batch, **kw)
     prob = TMzAdjoint(space, geom, src, design, monitor, nsteps, batch=batch,
-                      precision=precision, segment=segment)
+                      precision=precision, segment=segment, keep_history=keep_history)
     return prob, eps, (space, geom, src, design, monitor, nsteps)
 
 
@@ -113,6 +113,26 @@ def test_adjoint_matches_central_differences():
     rel = np.abs(ga - fd) / np.abs(fd)
     print("adjoint vs central differences, max relative error", rel.max())
     assert rel.max() <= 1e-4
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "df64"])
+def test_recorded_history_equals_checkpoint_recompute(precision):
+    """The forward that records every step's design increments (no backward
+    recompute) and the √N-checkpoint forward give the same J and gradient,
+    bit for bit; the default picks the recorded history when it fits."""
+    a, eps, _ = make(precision, batch=2, keep_history=True)
+    b, _, _ = make(precision, batch=2, keep_history=False)
+    assert a.keep_history and not b.keep_history
+    assert make(precision)[0].keep_history  # a small problem: fits
+    assert not make(precision, segment=9)[0].keep_history
+    Ja, Jb = a.forward(eps).cpu().numpy(), b.forward(eps).cpu().numpy()
+    assert np.array_equal(Ja, Jb)
+    ga, gb = a.backward().cpu().numpy(), b.backward().cpu().numpy()
+    assert np.abs(ga).max() > 0
+    assert np.array_equal(ga, gb)
+    # a second forward / backward on the same problem reuses its buffers
+    a.forward(eps[::-1].copy())
+    assert not np.array_equal(a.backward().cpu().numpy(), ga)
 
 
 def test_checkpoint_segments_do_not_change_the_gradient():

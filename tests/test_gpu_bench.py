@@ -36,12 +36,16 @@ def test_cube_line():
     assert d["gpu_launches"] > 0
 
 
-def test_design_line():
+@pytest.mark.parametrize("segment,passes", [(0, 2), (45, 3)])
+def test_design_line(segment, passes):
+    """Recorded history (forward + adjoint) and √N checkpoints (forward,
+    recompute, adjoint): the line counts the passes that ran."""
     d = bench("--workload", "design2d", "--n", "160", "--batch", "2", "--steps", "1",
-              "--warmup", "1", "--no-cpu-baseline")
+              "--warmup", "1", "--no-cpu-baseline", "--segment", str(segment))
     per = d["forward_s"] + d["backward_s"]
     assert d["ms_per_step"] == pytest.approx(per * 1e3, rel=1e-3)
     assert d["gradients_per_s"] == pytest.approx(2 / per, rel=1e-3)
     cells, steps = 160 * 160, d["config"]["time_steps"]
-    assert d["value"] == pytest.approx(3 * cells * steps * 2 / per / 1e9, rel=1e-3)
-    assert d["grad_finite"]
+    assert d["value"] == pytest.approx(passes * cells * steps * 2 / per / 1e9, rel=1e-3)
+    assert (d["config"]["checkpoints"] == 0) == (passes == 2)
+    assert d["grad_finite"] and d["gpu_launches"] > 0
