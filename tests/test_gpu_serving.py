@@ -120,8 +120,30 @@ def test_server_admission_respects_memory_budget_and_survives_bad_jobs():
     assert server.used_bytes == 0
 
 
+@pytest.mark.parametrize("fill_cells,most", [(1, 1), (9000, 3), (0, 6)])
+def test_server_fill_limit(fill_cells, most):
+    """Jobs wait while the resident grids hold ``fill_cells`` cells (one is
+    always admitted); results do not depend on it."""
+    builds = mix()
+    jobs = [Job(arrival=0.0, jid=i, build=b, nsteps=n, keep_fields=True)
+            for i, (b, n) in enumerate(builds)]
+    server = Server(precision="fp64", chunk=16, fill_cells=fill_cells)
+    rep = server.run(jobs, realtime=False)
+    assert rep["jobs"] == len(jobs) and rep["failed"] == 0
+    assert 1 <= rep["max_resident"] <= most
+    if fill_cells == 0:
+        assert rep["max_resident"] == len(jobs)
+    assert server.resident_cells == 0
+    for job in server.finished:
+        b, n = builds[job.jid]
+        ref = alone(b, n, "fp64")
+        for c in range(6):
+            assert np.array_equal(job.fields[c], ref[c]), (fill_cells, job.jid, c)
+
+
 def test_one_at_a_time_baseline_runs():
     builds = mix()[:2]
     jobs = [Job(arrival=0.0, jid=i, build=b, nsteps=n) for i, (b, n) in enumerate(builds)]
     rep = run_one_at_a_time(jobs)
     assert rep["cell_updates"] > 0 and rep["gcells_per_s"] > 0
+    assert rep["latency_p99_s"] >= rep["latency_p50_s"] > 0
