@@ -87,8 +87,9 @@ __device__ __forceinline__ Pre<P> prefetch_state(const GridDev& g, int64_t lin, 
 // Whether the CPML psi updates run behind a warp-wide vote.  Measured on
 // GB300 (256^3 cube): FP64 13.58 -> 14.18 Gcell/s (19.0 -> 17.6 FP64
 // instructions per cell) and FP32 31.2 -> 32.7; the float-float type runs
-// slower with it (19.6 -> 18.3).  Votes in front of the other kinds' blocks
-// were slower in every precision.
+// slower with it (19.6 -> 18.3; with a __syncwarp opening each voted block
+// and 16-cell rows, 21.05 -> 20.67).  Votes in front of the other kinds'
+// blocks were slower in every precision.
 template <class P>
 struct PsiVote {
   static constexpr bool value = true;
