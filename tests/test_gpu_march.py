@@ -106,3 +106,27 @@ def test_full_size_cube256_against_strict():
         del sim
     print("full-size relative L2 vs reference-order FP64:", errs)
     assert errs["fp64"] <= 1e-12 and errs["df64"] <= 1e-12 and errs["fp32"] <= 5e-3
+
+
+def test_full_size_dispersive192_against_strict():
+    """192^3 dispersive scene (Drude / Lorentz / DCP-ADE spheres, UPML, TFSF
+    plane wave), 600 steps through the pulse peak: fp64 within 1e-12 and
+    df64 within 1e-11 of the reference-order FP64 run, fp32 error recorded."""
+    steps = 600
+    build = lambda p: W.dispersive(192, precision=p, src_time=PULSE)
+    strict = _run(build, "fp64_strict", steps)
+    ref = [strict.field[c].tensor() for c in G.constant.COMPONENTS]
+    assert max(float(r.abs().max()) for r in ref) > 1e-6
+    del strict
+    errs = {}
+    for prec in ("fp64", "df64", "fp32"):
+        sim = _run(build, prec, steps)
+        e = 0.0
+        for c, comp in enumerate(G.constant.COMPONENTS):
+            got = sim.field[comp].tensor()
+            nb = float(ref[c].norm())
+            e = max(e, float((got - ref[c]).norm()) / nb if nb else 0.0)
+        errs[prec] = e
+        del sim
+    print("dispersive 192^3 relative L2 vs reference-order FP64:", errs)
+    assert errs["fp64"] <= 1e-12 and errs["df64"] <= TOL["df64"] and errs["fp32"] <= TOL["fp32"]
