@@ -25,7 +25,17 @@
 namespace gmes {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;  // multi-grid kernels (tiles of the batch workspace)
+// Threads per block of the single-grid cell kernel (16 cells along k by 8
+// rows).  Measured on GB300, Gcell/s at 128 / 256 / 512 threads (the same
+// registers and resident warps per SM):
+//   256^3 cube        FP64 17.34 / 16.70 / 14.97   FP32 33.66 / 33.42   df64 21.80 / 20.98
+//   192^3 dispersive  FP64  9.81 /  9.36 /  8.70   FP32 20.26 / 19.85   df64 14.76 / 13.75
+// GMES_CELL_THREADS overrides it (tuning builds).
+#ifndef GMES_CELL_THREADS
+#define GMES_CELL_THREADS 128
+#endif
+constexpr int kCellThreads = GMES_CELL_THREADS;
 // Resident blocks per SM the cell kernels' register budget targets.
 // Measured on GB300 (256^3 cube): FP32 runs 8% faster at 5 blocks (48
 // registers) than at 4 (56); 6 and 8 blocks spill and run slower.  FP64
@@ -644,21 +654,29 @@ __device__ __forceinline__ void cell_body(const GridDev& g, int i, int j, int k)
   }
 }
 
+// The register budget of MinBlocks (blocks of 256 threads) in blocks of
+// kCellThreads.
+template <class P>
+struct CellMinBlocks {
+  static constexpr int value = MinBlocks<P>::value * 256 / kCellThreads;
+};
+
 template <class P, int SIDE, bool STRICT, bool DISP, int MASK, class I>
-__global__ void __launch_bounds__(kThreads, MinBlocks<P>::value)
+__global__ void __launch_bounds__(kCellThreads, CellMinBlocks<P>::value)
     k_cell(const GridDev g, int bx_log2, int i0) {
   const int bx = 1 << bx_log2;
   const int tx = threadIdx.x & (bx - 1);
   const int ty = threadIdx.x >> bx_log2;
   const int k = blockIdx.x * bx + tx;
-  const int j = blockIdx.y * (kThreads >> bx_log2) + ty;
+  const int j = blockIdx.y * (kCellThreads >> bx_log2) + ty;
   const int i = i0 + (int)blockIdx.z;
   if (k >= g.n[2] || j >= g.n[1] || i >= g.n[0]) return;
   cell_body<P, SIDE, STRICT, DISP, MASK, I>(g, i, j, k);
 }
 
 // Cells per block row along k (log2): a warp covers 16 cells of two rows
-// (128 bytes per row in FP64 and df64, 64 in FP32).  Against 32 cells of
+// (128 bytes per row in FP64 and df64, 64 in FP32).  (Measured with blocks
+// of 256 threads.)  Against 32 cells of
 // one row, a warp straddles a material or CPML edge along k in half as many
 // places, so fewer warps run two kinds' code or a psi block for a few
 // lanes.  Measured on GB300, Gcell/s, rows of 32 / 16 / 8 cells:
@@ -677,11 +695,11 @@ void launch_cell(const GridDev& d, int side, bool disp, dim3 grid, int bx_log2, 
                  cudaStream_t s) {
   if (side == 0) {
     if (disp)
-      k_cell<P, 0, STRICT, true, MASK, I><<<grid, kThreads, 0, s>>>(d, bx_log2, i0);
+      k_cell<P, 0, STRICT, true, MASK, I><<<grid, kCellThreads, 0, s>>>(d, bx_log2, i0);
     else
-      k_cell<P, 0, STRICT, false, MASK, I><<<grid, kThreads, 0, s>>>(d, bx_log2, i0);
+      k_cell<P, 0, STRICT, false, MASK, I><<<grid, kCellThreads, 0, s>>>(d, bx_log2, i0);
   } else {
-    k_cell<P, 1, STRICT, false, MASK, I><<<grid, kThreads, 0, s>>>(d, bx_log2, i0);
+    k_cell<P, 1, STRICT, false, MASK, I><<<grid, kCellThreads, 0, s>>>(d, bx_log2, i0);
   }
 }
 
@@ -987,7 +1005,7 @@ void run_half(const Plan& p, int side, int st, cudaStream_t s) {
     k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
   int bx_log2 = 0;
   while (bx_log2 < kRowLog2 && (1 << bx_log2) < d.n[2]) ++bx_log2;
-  const int bx = 1 << bx_log2, by = kThreads / bx;
+  const int bx = 1 << bx_log2, by = kCellThreads / bx;
   const int nplanes = p.cplx ? 2 : 1;
   for (int part = 0; part < nplanes; ++part) {
     const GridDev& v = part == 0 ? p.re : p.im;
