@@ -588,7 +588,7 @@ def run_design(args):
                    "precision": precision, "block_steps": args.block_steps,
                    "l2": "state 7 x batch x n^2 x elem > L2 for batch 64 (inputs larger than L2)"},
         "gradients_per_s": round(args.batch / per, 3),
-        "forward_s": round(tf, 4), "backward_s": round(tb, 4),
+        "forward_s": round(tf, 6), "backward_s": round(tb, 6),
         "forward_alg_GBps": round(fwd_gbs, 1), "backward_alg_GBps": round(bwd_gbs, 1),
         "hbm_peak_GBps": peak[0] if peak else None,
         # the forward pass against HBM: algorithmic bytes of a one-step
