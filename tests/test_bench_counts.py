@@ -1,0 +1,44 @@
+"""Host-side figures of the bench line that need no GPU: the kernel-launch
+count claimed for the differentiation workload, which follows the
+library's chunking of the temporally blocked kernels."""
+import types
+
+import pytest
+
+
+def _prob(nsteps, segment, keep):
+    return types.SimpleNamespace(nsteps=nsteps, segment=segment, keep_history=keep)
+
+
+def _adj_chunks(k, per):
+    # the library's adjoint chunks: odd counts of at most ``per`` steps
+    n = 0
+    while k > 0:
+        m = min(k, per)
+        if m % 2 == 0:
+            m -= 1
+        k -= m
+        n += 1
+    return n
+
+
+@pytest.mark.parametrize("nsteps,segment", [(2000, 45), (160, 7), (37, 37), (1, 1)])
+def test_design_launch_count(nsteps, segment):
+    import bench
+    per = 4
+    segs = [min(segment, nsteps - s0) for s0 in range(0, nsteps, segment)]
+    fwd = sum(-(-k // per) for k in segs)
+    # √N checkpoints: forward and recompute per segment, then the adjoint
+    assert bench.design_launches(_prob(nsteps, segment, False), "fp32", 0) == \
+        2 * fwd + sum(_adj_chunks(k, per) for k in segs)
+    # recorded history: one forward and one adjoint over all steps
+    assert bench.design_launches(_prob(nsteps, segment, True), "fp32", 0) == \
+        -(-nsteps // per) + _adj_chunks(nsteps, per)
+    # one step per launch: E, E sources, H, H sources per step of each pass
+    assert bench.design_launches(_prob(nsteps, segment, True), "fp64", 0) == 8 * nsteps
+    assert bench.design_launches(_prob(nsteps, segment, False), "fp32", 1) == 12 * nsteps
+
+
+def test_adjoint_chunks_of_the_default_workload():
+    # 2000 steps: 666 launches of 3 steps, then two of 1
+    assert _adj_chunks(2000, 4) == 668
