@@ -75,6 +75,12 @@ def build(verbose=False, jobs=None):
     tmp = LIB.with_suffix(".so.tmp")
     run([exe, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"])
     os.replace(tmp, LIB)
+    # objects of earlier sources or flags are not needed again
+    keep = set(objs)
+    for name in SOURCES:
+        for old in BUILD.glob(f"{Path(name).stem}-*.o"):
+            if old not in keep:
+                old.unlink()
     return LIB
 
 
