@@ -6,7 +6,7 @@ of ``cases.py`` and stores the resulting fields with the reference's time
 bookkeeping.  The tests compare the CPU oracle and the CUDA engine against
 these files; they never need the reference itself.
 
-Usage:  python tests/golden/make_golden.py [case ...]
+Usage:  python tests/golden/make_golden.py [case ...]   (cases.CASES and cases.ORACLE_CASES)
         python tests/golden/make_golden.py --probes [case ...]
         python tests/golden/make_golden.py --pw
 """
@@ -24,7 +24,9 @@ ROOT = HERE.parents[1]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(HERE))
 
-from cases import CASES, COMP_NAMES, SUMMARY_ONLY  # noqa: E402
+from cases import CASES, COMP_NAMES, ORACLE_CASES, SUMMARY_ONLY  # noqa: E402
+
+ALL_CASES = {**CASES, **ORACLE_CASES}
 
 
 def checksum(a):
@@ -42,7 +44,7 @@ def main(names):
     gmes = load_reference()
     for name in names:
         t0 = time.time()
-        sim, nsteps = CASES[name](gmes)
+        sim, nsteps = ALL_CASES[name](gmes)
         sim.init()
         t1 = time.time()
         for _ in range(nsteps):
@@ -116,4 +118,4 @@ if __name__ == "__main__":
     elif args[:1] == ["--probes"]:
         probes(args[1:] or list(PROBES))
     else:
-        main(args or list(CASES))
+        main(args or list(ALL_CASES))

@@ -10,15 +10,18 @@ import numpy as np
 import pytest
 
 import gmes_gb300 as G
-from cases import CASES, COMP_NAMES, SUMMARY_ONLY
+from cases import CASES, COMP_NAMES, ORACLE_CASES, SUMMARY_ONLY
 from conftest import checksum, load_golden
 from oracle.oracle import Oracle
 
 
-@pytest.mark.parametrize("name", list(CASES))
+ALL_CASES = {**CASES, **ORACLE_CASES}
+
+
+@pytest.mark.parametrize("name", list(ALL_CASES))
 def test_oracle_matches_reference_bitwise(name):
     gold, meta = load_golden(name)
-    sim, nsteps = CASES[name](G)
+    sim, nsteps = ALL_CASES[name](G)
     assert nsteps == meta["steps"]
     scene = sim.compile()
     orc = Oracle(scene)
