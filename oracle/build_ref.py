@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY: the product never imports, links or runs what this
 builds.  The build reads the reference sources where they lie (the
-reference checkout, default ``/root/reference``) and writes only into
-``oracle/_ref/`` (git-ignored):
+reference checkout named by ``--ref`` or the ``GMES_REFERENCE`` environment
+variable) and writes only into ``oracle/_ref/`` (git-ignored):
 
 * ``src/pygeom.pyx`` and ``src/material.pyx`` are cythonized and compiled
   unmodified, as ``gmes.pygeom`` and ``gmes.material``;
@@ -20,7 +20,8 @@ path of ``oracle/_ref/gmes_ext`` followed by the reference's own ``gmes/``
 directory.  Only possible where the reference tree, Cython and pybind11 are
 present (the build container); the GPU host has neither.
 
-Usage: ``python oracle/build_ref.py [--ref /root/reference]``.
+Usage: ``GMES_REFERENCE=<reference checkout> python oracle/build_ref.py``
+or ``python oracle/build_ref.py --ref <reference checkout>``.
 """
 
 import argparse
@@ -44,6 +45,12 @@ _m = _u.module_from_spec(_s)
 _s.loader.exec_module(_m)
 globals().update({k: getattr(_m, k) for k in dir(_m) if not k.startswith("__")})
 '''
+
+
+def reference_from_env():
+    """The reference checkout named by GMES_REFERENCE, or None when it is unset."""
+    v = os.environ.get("GMES_REFERENCE", "").strip()
+    return Path(v) if v else None
 
 
 def _run(cmd):
@@ -88,6 +95,10 @@ def build(ref: Path, jobs: int = 4) -> Path:
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--ref", default=os.environ.get("GMES_REFERENCE", "/root/reference"))
+    ap.add_argument("--ref", default=None,
+                    help="reference checkout (default: the GMES_REFERENCE environment variable)")
     args = ap.parse_args()
-    print(build(Path(args.ref)))
+    ref = Path(args.ref) if args.ref else reference_from_env()
+    if ref is None:
+        sys.exit("no reference checkout: pass --ref or set GMES_REFERENCE")
+    print(build(ref))

@@ -16,14 +16,18 @@ EXT = HERE / "_ref" / "gmes_ext"
 
 
 def reference_root():
+    """The checkout the build read (recorded in oracle/_ref/REF_PATH), else
+    GMES_REFERENCE; None when neither names one."""
     p = HERE / "_ref" / "REF_PATH"
     if p.exists():
         return Path(p.read_text().strip())
-    return Path(os.environ.get("GMES_REFERENCE", "/root/reference"))
+    v = os.environ.get("GMES_REFERENCE", "").strip()
+    return Path(v) if v else None
 
 
 def available():
-    return (EXT / "constant.py").exists() and (reference_root() / "gmes" / "fdtd.py").exists()
+    root = reference_root()
+    return (EXT / "constant.py").exists() and root is not None and (root / "gmes" / "fdtd.py").exists()
 
 
 def load_reference():
