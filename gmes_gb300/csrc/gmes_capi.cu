@@ -1041,10 +1041,31 @@ static_assert(GMES_NOALLOC_MAX_GRIDS * sizeof(GridDev) + 8192 <= kNoAllocBytes,
 // symbol directly: its device address comes from cudaGetSymbolAddress.
 __device__ __align__(256) char g_noalloc_tables[kNoAllocBytes];
 
+// The tables reach the device as launch arguments of k_noalloc_fill, one
+// piece of at most kTableChunk bytes per launch (a launch copies its
+// arguments when it is enqueued), so no host buffer has to outlive the call
+// and nothing waits for earlier work on the stream.
+constexpr int kTableChunk = 24 * 1024;
+struct TableChunk {
+  int64_t offset;  // byte offset into the fixed array
+  int32_t words;   // 16-byte words in data
+  int32_t pad;
+  uint4 data[kTableChunk / 16];
+};
+static_assert(sizeof(TableChunk) <= 32000, "kernel arguments are limited to 32764 bytes");
+static_assert(kNoAllocBytes % 16 == 0 && kTableChunk % 256 == 0, "16-byte words");
+
+__global__ void k_noalloc_fill(char* dst, const __grid_constant__ TableChunk c) {
+  uint4* out = reinterpret_cast<uint4*>(dst + c.offset);
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < c.words; w += gridDim.x * blockDim.x)
+    out[w] = c.data[w];
+}
+
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 void* g_noalloc_addr[kMaxDevices] = {};          // per device, looked up on first use
 alignas(256) char g_noalloc_image[kNoAllocBytes];  // host image, guarded by the mutex
+TableChunk g_noalloc_chunk;                        // launch argument, guarded by the mutex
 
 }  // namespace
 }  // namespace gmes
@@ -1087,7 +1108,7 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
   for (int q = 0; q < njobs; ++q) {
     const gmes_grid_desc* g = grids[q];
     gmes_status st = check_desc(g, true);
-    if (st != GMES_OK) return st;
+    if (st != GMES_OK) return fail(st, "grid %d: %s", q, g_last_error.c_str());
     if (g->ntfsf > 0) return fail(GMES_ERR_VALUE, "grid %d has a TFSF source: not batchable", q);
     if (g->nprobe > 0) return fail(GMES_ERR_VALUE, "grid %d has probes: not batchable", q);
     if (g->flags & GMES_FLAG_COMPLEX)
@@ -1116,10 +1137,18 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
     stp[q] = steps[q];
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // pageable source: the call returns once the image is staged, so the host
-  // image can be rebuilt by the next call
-  e = cudaMemcpyAsync(g_noalloc_addr[dev], img, (size_t)L.total, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(e, "uploading the fixed batch table");
+  char* dst = static_cast<char*>(g_noalloc_addr[dev]);
+  for (int64_t off = 0; off < L.total; off += kTableChunk) {
+    TableChunk& c = g_noalloc_chunk;
+    const int64_t bytes = L.total - off < kTableChunk ? L.total - off : kTableChunk;
+    c.offset = off;
+    c.words = (int32_t)(bytes / 16);
+    c.pad = 0;
+    std::memcpy(c.data, img + off, (size_t)bytes);
+    k_noalloc_fill<<<8, 256, 0, s>>>(dst, c);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "uploading the fixed batch table");
+  }
   gmes_batch b;
   b.njobs = njobs;
   b.precision = precision;

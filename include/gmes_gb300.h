@@ -351,7 +351,9 @@ gmes_status gmes_batch_step(const gmes_batch* b, int32_t nsteps, int32_t blocks,
  * call rebuilds the tables for `grids` (same rules as gmes_batch_prepare),
  * then advances grid g by steps[g] of the nsteps steps (same as
  * gmes_batch_set_steps + gmes_batch_step), reading each grid's staged
- * source values.
+ * source values.  The tables reach that array as the launch arguments of
+ * small copy kernels enqueued on `stream`, so the call does not wait for
+ * earlier work on the stream and no host buffer outlives it.
  *   - The first call on a device also looks up that array's device address
  *     (with the device current); make that first call before any stream
  *     capture.

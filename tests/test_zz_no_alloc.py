@@ -8,9 +8,11 @@ identical sets of grids, one through gmes_batch_prepare / gmes_batch_set_steps
 / gmes_batch_step with a workspace, the other through
 gmes_batch_step_noalloc, both through the C ABI, and requires the same
 fields (the batch kernels are deterministic, so the tolerance is exact
-equality) after each of two calls in a row.  It builds everything it needs
-itself, so it passes alone in a fresh process as well as after the rest of
-the suite.
+equality) after each of three calls in a row (the third with a narrower
+block shape, which changes only how the cells are split into blocks).  The
+device's free memory is the same before and after a call once the kernels
+are loaded.  It builds everything it needs itself, so it passes alone in a
+fresh process as well as after the rest of the suite.
 """
 import ctypes as C
 
@@ -57,16 +59,21 @@ def test_noalloc_batch_matches_workspace_batch():
     N.check(lib.gmes_batch_prepare(desc_a, n, C.c_void_p(ws.data_ptr()), ws_bytes, 0,
                                    C.byref(batch), C.c_void_p(stream.cuda_stream)))
     done = [0] * n
-    for call, steps in enumerate(([13, 7, 20], [5, 12, 9])):
+    for call, (steps, bx_cap) in enumerate((([13, 7, 20], 0), ([5, 12, 9], 0),
+                                            ([8, 3, 11], 3))):
         k = max(steps)
         stage(a, steps, done)
         stage(b, steps, done)
         st = (C.c_int32 * n)(*steps)
         N.check(lib.gmes_batch_set_steps(C.byref(batch), st, C.c_void_p(stream.cuda_stream)))
         N.check(lib.gmes_batch_step(C.byref(batch), k, 0, C.c_void_p(stream.cuda_stream)))
-        N.check(lib.gmes_batch_step_noalloc(desc_b, st, n, k, 0,
+        stream.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        N.check(lib.gmes_batch_step_noalloc(desc_b, st, n, k, bx_cap,
                                             C.c_void_p(stream.cuda_stream)))
         stream.synchronize()
+        if call > 0:  # the first call also loads the kernels
+            assert torch.cuda.mem_get_info()[0] == free0, call
         done = [d + s for d, s in zip(done, steps)]
         for q in range(n):
             for c in range(6):
@@ -84,3 +91,13 @@ def test_noalloc_rejects_more_grids_than_its_table_holds():
     steps = (C.c_int32 * n)(*([1] * n))
     with pytest.raises(ValueError, match="capacity"):
         N.check(lib.gmes_batch_step_noalloc(descs, steps, n, 1, 0, None))
+
+
+def test_noalloc_rejects_steps_beyond_the_staged_source_values():
+    lib = N.load()
+    e = GridEngine(grids()[0].compile(), src_chunk=8)
+    assert e.desc.nsrc > 0
+    descs = (C.POINTER(N.GridDescC) * 1)(C.pointer(e.desc))
+    steps = (C.c_int32 * 1)(9)
+    with pytest.raises(ValueError, match="source-value capacity"):
+        N.check(lib.gmes_batch_step_noalloc(descs, steps, 1, 9, 0, None))
