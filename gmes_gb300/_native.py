@@ -14,7 +14,7 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ["GMES_GB300_LIB"]) if os.environ.get("GMES_GB300_LIB") else \
     PKG / "libgmes_gb300.so"
 
-ABI_VERSION = 5
+ABI_VERSION = 6
 MAX_CLASSES = 256
 MAX_PML = 4
 MAX_POLES = 8
@@ -22,6 +22,7 @@ MAX_POLES = 8
 FP64, FP32, DF64, FP64_STRICT = 0, 1, 2, 3
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "df64": DF64, "fp64_strict": FP64_STRICT}
 FLAG_DISPERSIVE = 1
+FLAG_POINTWISE = 4
 FLAG_COMPLEX = 2
 
 EXPORTS = [
@@ -34,7 +35,7 @@ EXPORTS = [
     "gmes_graph_destroy", "gmes_rasterize", "gmes_batch_step_noalloc",
     "gmes_tmz_sizes", "gmes_tmz_check", "gmes_tmz_set_design", "gmes_tmz_reset",
     "gmes_tmz_forward", "gmes_tmz_objective", "gmes_tmz_adjoint", "gmes_points_update",
-    "gmes_copy_async",
+    "gmes_copy_async", "gmes_nonfinite",
 ]
 NOALLOC_MAX_GRIDS = 64
 
@@ -182,6 +183,7 @@ def load():
                                    C.c_void_p]
     lib.gmes_graph_destroy.argtypes = [C.c_void_p]
     lib.gmes_copy_async.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.gmes_nonfinite.argtypes = [P(GridDescC), C.c_void_p, C.c_void_p]
     G, B = P(GridDescC), P(TmzBatchC)
     lib.gmes_tmz_sizes.argtypes = [G, B, P(C.c_int64)]
     lib.gmes_tmz_check.argtypes = [G, B]

@@ -6,11 +6,10 @@ of the persistent kernel (``blocks``; 0 = one block per tile).  Which is
 best depends on the mix of grid shapes (thin 2-D grids want short k extents,
 large 3-D grids want full warps along k and enough blocks to hide memory
 latency).  The tuner measures candidates on live chunks -- every candidate
-computes exactly the same values, so tuning costs no extra work -- and
-keeps the fastest per mix bucket.
+computes exactly the same values, so tuning costs no extra work -- timing
+each chunk on the device (CUDA events around its launches on the batch's
+stream), and keeps the fastest per mix bucket.
 """
-
-import time
 
 
 def _sms():
@@ -24,14 +23,16 @@ class Tuner:
 
     def __init__(self, candidates=None, trials_per_candidate=1):
         sms = _sms()
+        # block extent along k (2^bx_cap cells) x persistent grid size
+        # (0: one block per tile; else a multiple of the SM count)
         self.candidates = candidates or [
-            (5, 0), (4, 0), (3, 0), (5, 8 * sms), (5, 32 * sms), (4, 16 * sms)]
+            (bx, blocks) for bx in (4, 5, 3) for blocks in (0, 12 * sms, 24 * sms, 48 * sms)]
         self.trials_per_candidate = int(trials_per_candidate)
         self.best = {}
         self.results = {}
         self._key = None
         self._cand = None
-        self._t0 = None
+        self._ev = None
 
     @staticmethod
     def bucket(jobs):
@@ -64,15 +65,31 @@ class Tuner:
         return self._cand
 
     def observe_start(self, batch):
-        self._t0 = time.perf_counter()
+        """Before a chunk's launches: a start event on the batch's stream
+        (only while the bucket is still being explored)."""
+        self._ev = None
+        if self._key is None or self._key in self.best:
+            return
+        from .engine import _torch
+        torch = _torch()
+        self._ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        self._ev[0].record(batch.stream)
+
+    def observe_stop(self, batch):
+        """After the chunk's launches: the end event."""
+        if self._ev is not None:
+            self._ev[1].record(batch.stream)
 
     def observe_end(self, batch, cell_updates):
-        if self._t0 is None or self._key is None or self._key in self.best:
+        """After the chunk has completed: record its device-timed throughput."""
+        if self._ev is None:
             return
-        dt = time.perf_counter() - self._t0
+        ms = self._ev[0].elapsed_time(self._ev[1])
+        self._ev = None
         cand = (batch.bx_cap, batch.blocks)
-        if dt > 0:
-            self.results.setdefault(self._key, {}).setdefault(cand, []).append(cell_updates / dt)
+        if ms > 0:
+            self.results.setdefault(self._key, {}).setdefault(cand, []).append(
+                cell_updates / (ms / 1e3))
 
     def summary(self):
         return {str(k): {"best": v, "measured": {str(c): max(r) for c, r in

@@ -129,6 +129,7 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
   d.dt = g.dt;
   d.active = g.active;
   d.nsrc = g.nsrc;
+  d.pointwise = (g.flags & GMES_FLAG_POINTWISE) ? 1 : 0;
   const CoefLayout L = coef_layout(g);
   char* base = static_cast<char*>(g.coef);
   for (int c = 0; c < 6; ++c) {
@@ -148,6 +149,13 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
       for (int a = 0; a < 3; ++a)
         d.prof[p][c][a] = reinterpret_cast<const Coef*>(base + L.prof[p][c][a]);
   }
+  const int64_t n1 = g.n[1], n2 = g.n[2];
+  d.fst[0][0] = (n1 + 1) * (n2 + 1);
+  d.fst[0][1] = n2 + 1;
+  d.fst[1][0] = n1 * (n2 + 1);
+  d.fst[1][1] = n2 + 1;
+  d.fst[2][0] = (n1 + 1) * n2;
+  d.fst[2][1] = n2;
   d.src = g.src;
   d.src_val = g.src_val;
   std::memcpy(d.phase, g.bloch_phase, sizeof(d.phase));
@@ -672,6 +680,16 @@ gmes_status gmes_rasterize(const gmes_grid_desc* g, int32_t comp, const gmes_sha
   cudaError_t e = launch_raster(*g, d, comp, shapes, nshapes, lut,
                                 static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching the rasteriser");
+  return GMES_OK;
+}
+
+gmes_status gmes_nonfinite(const gmes_grid_desc* g, int32_t* flag, void* stream) {
+  gmes_status st = check_desc(g, true);
+  if (st != GMES_OK) return st;
+  if (flag == nullptr) return fail(GMES_ERR_VALUE, "flag is NULL");
+  const GridDev d = make_grid_dev(*g);
+  cudaError_t e = launch_nonfinite(*g, d, flag, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "launching the non-finite check");
   return GMES_OK;
 }
 

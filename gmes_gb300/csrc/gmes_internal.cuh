@@ -80,6 +80,37 @@ __host__ __device__ inline void comp_shape(const int32_t n[3], int32_t active, i
 
 __host__ __device__ inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
 
+// ---------------------------------------------------------------------------
+// Block tiling of the single-grid cell kernels.  A block of kCellThreads
+// threads covers bx cells along k (bx = 2^bx_log2, at most 2^kRowLog2, the
+// smallest power of two >= n2 below that) by kCellThreads / bx rows along j,
+// at one i; blocks are numbered ((i * njb) + jb) * nkb + kb.  Warp w of a
+// block covers its threads 32 w .. 32 w + 31.
+// ---------------------------------------------------------------------------
+#ifndef GMES_CELL_THREADS
+#define GMES_CELL_THREADS 128
+#endif
+constexpr int kCellThreads = GMES_CELL_THREADS;
+constexpr int kCellWarps = kCellThreads / 32;
+constexpr int kRowLog2 = 4;
+
+struct CellTiling {
+  int bx_log2, bx, by, nkb, njb;
+  int64_t blocks;  // nkb * njb * n0
+};
+
+__host__ __device__ inline CellTiling cell_tiling(const int32_t n[3]) {
+  CellTiling t;
+  t.bx_log2 = 0;
+  while (t.bx_log2 < kRowLog2 && (1 << t.bx_log2) < n[2]) ++t.bx_log2;
+  t.bx = 1 << t.bx_log2;
+  t.by = kCellThreads / t.bx;
+  t.nkb = (n[2] + t.bx - 1) / t.bx;
+  t.njb = (n[1] + t.by - 1) / t.by;
+  t.blocks = (int64_t)t.nkb * t.njb * n[0];
+  return t;
+}
+
 // Coefficient block layout (offsets in bytes from g.coef).
 struct CoefLayout {
   int64_t raw_classes;  // gmes_class_desc[sum nclass] (host input staging)
@@ -133,7 +164,7 @@ struct GridDev {
   int32_t n[3];
   int32_t active;
   int32_t nsrc;
-  int32_t pad;
+  int32_t pointwise;      // GMES_FLAG_POINTWISE: no warp-uniform plain updates
   int64_t sh[6][3];       // component shapes
   int64_t st[6][2];       // strides of axes 0 and 1 (axis 2 stride is 1)
   int64_t npts[6];        // points per component
@@ -164,6 +195,10 @@ struct GridDev {
   double phase[6][2][2];   // Bloch phase factors (complex grids)
   int32_t part;            // 0: real plane, 1: imaginary plane (complex grids)
   int32_t pad4;
+  // strides of axes 0 and 1 of the three array shapes: X = Ex/Hx
+  // (n0, n1+1, n2+1), Y = Ey/Hy (n0+1, n1, n2+1), Z = Ez/Hz (n0+1, n1+1, n2);
+  // an active component's strides are its family's
+  int64_t fst[3][2];
 };
 
 // Host-side launch plan of one grid: its real-plane view, the imaginary-
@@ -271,8 +306,9 @@ __device__ __forceinline__ double to_double(double v) { return v; }
 __device__ __forceinline__ double to_double(float v) { return (double)v; }
 __device__ __forceinline__ double to_double(df v) { return (double)v.hi + (double)v.lo; }
 
-// Threads per block of the half-step kernels (single grid and batch).
-constexpr int kBatchThreads = 256;
+// Threads per block of the multi-grid half-step kernel: the single-grid
+// kernel's shape.
+constexpr int kBatchThreads = kCellThreads;
 
 // Kernel-side view of a batch workspace (gmes_batch_prepare).
 // True when every component of the grid holds fewer than 2^31 points, so
@@ -379,5 +415,7 @@ cudaError_t launch_raster(const gmes_grid_desc& gd, const GridDev& d, int c,
                           cudaStream_t s);
 cudaError_t launch_build_coefficients(const gmes_grid_desc& g, const GridDev& d,
                                       cudaStream_t s);
+cudaError_t launch_nonfinite(const gmes_grid_desc& g, const GridDev& d, int32_t* flag,
+                             cudaStream_t s);
 
 }  // namespace gmes

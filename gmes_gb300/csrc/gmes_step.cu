@@ -25,38 +25,43 @@
 namespace gmes {
 namespace {
 
-constexpr int kThreads = 256;  // multi-grid kernels (tiles of the batch workspace)
-// Threads per block of the single-grid cell kernel (16 cells along k by 8
-// rows).  Measured on GB300, Gcell/s at 128 / 256 / 512 threads (the same
-// registers and resident warps per SM):
+// Threads per block of the cell kernels, single-grid and multi-grid:
+// kCellThreads (16 cells along k by 8 rows).  Measured on GB300, Gcell/s at
+// 128 / 256 / 512 threads (the same registers and resident warps per SM):
 //   256^3 cube        FP64 17.34 / 16.70 / 14.97   FP32 33.66 / 33.42   df64 21.80 / 20.98
 //   192^3 dispersive  FP64  9.81 /  9.36 /  8.70   FP32 20.26 / 19.85   df64 14.76 / 13.75
 // GMES_CELL_THREADS overrides it (tuning builds).
-#ifndef GMES_CELL_THREADS
-#define GMES_CELL_THREADS 128
+//
+// Resident blocks per SM the cell kernels' register budget targets (blocks
+// of 128 threads).  Measured on GB300 with the warp-uniform plain path
+// (256^3 cube, Gcell/s):
+//   FP64  7 blocks (72 registers) 17.29   8 (64) 18.48   9 (56) 18.90
+//   FP32  10 blocks (48) 34.31           11 (46) 39.40  12 (40) 39.42
+//   df64  7 blocks 20.44                 8 (64) 22.33   9 (56) 22.60
+// FP32 is bound by the loads in flight, so extra resident warps pay most
+// there; FP64 is bound by its pipe.  GMES_CELL_BLOCKS_F64 / _F32 / _DF
+// override them (tuning builds).
+#ifndef GMES_CELL_BLOCKS_F64
+#define GMES_CELL_BLOCKS_F64 9
 #endif
-constexpr int kCellThreads = GMES_CELL_THREADS;
-// Resident blocks per SM the cell kernels' register budget targets.
-// Measured on GB300 (256^3 cube): FP32 runs 8% faster at 5 blocks (48
-// registers) than at 4 (56); 6 and 8 blocks spill and run slower.  FP64
-// and df64 run best at 4 (64 registers): at 5 they spill and lose 5% and
-// 12%, at 3 (74-80 registers, no spills) FP64 loses 13% (16.17 -> 14.13
-// Gcell/s).  GMES_MIN_BLOCKS overrides every precision (tuning builds).
-#ifdef GMES_MIN_BLOCKS
+#ifndef GMES_CELL_BLOCKS_F32
+#define GMES_CELL_BLOCKS_F32 12
+#endif
+#ifndef GMES_CELL_BLOCKS_DF
+#define GMES_CELL_BLOCKS_DF 9
+#endif
 template <class P>
-struct MinBlocks {
-  static constexpr int value = GMES_MIN_BLOCKS;
-};
-#else
-template <class P>
-struct MinBlocks {
-  static constexpr int value = 4;
+struct CellMinBlocks {
+  static constexpr int value = GMES_CELL_BLOCKS_F64 * 128 / kCellThreads;
 };
 template <>
-struct MinBlocks<PolF32> {
-  static constexpr int value = 5;
+struct CellMinBlocks<PolF32> {
+  static constexpr int value = GMES_CELL_BLOCKS_F32 * 128 / kCellThreads;
 };
-#endif
+template <>
+struct CellMinBlocks<PolDF> {
+  static constexpr int value = GMES_CELL_BLOCKS_DF * 128 / kCellThreads;
+};
 
 template <int C>
 __device__ __forceinline__ int64_t stride_of(const GridDev& g, int axis) {
@@ -144,6 +149,24 @@ struct SharedCpml<PolF64> {
   static constexpr bool value = true;
 };
 
+// The plain update of a point (a dielectric class, or a CPML point outside
+// both of its slabs): E: (F + c1 D1) - c2 D2, H: (F + c2 D2) - c1 D1, with
+// both multiply-adds fused explicitly, so that the per-point path, the
+// uniform-tile path and the multi-grid kernels round identically.
+__device__ __forceinline__ double plain_e(double F, double c1, double c2, double p1, double p2) {
+  return __fma_rn(-c2, p2, __fma_rn(c1, p1, F));
+}
+__device__ __forceinline__ float plain_e(float F, float c1, float c2, float p1, float p2) {
+  return __fmaf_rn(-c2, p2, __fmaf_rn(c1, p1, F));
+}
+__device__ __forceinline__ df plain_e(df F, df c1, df c2, df p1, df p2) {
+  return (F + c1 * p1) - c2 * p2;
+}
+template <bool E, class R>
+__device__ __forceinline__ R plain_upd(R F, R c1, R c2, R p1, R p2) {
+  return E ? plain_e(F, c1, c2, p1, p2) : plain_e(F, c2, c1, p2, p1);
+}
+
 template <class P, int C, bool DISP>
 __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const int x[3],
                                             typename P::R p1, typename P::R p2,
@@ -175,7 +198,7 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
       }
       if (!scaled) {
         const R c1 = P::cfg(&(cc.c1)), c2 = P::cfg(&(cc.c2));
-        R t = E ? (F + c1 * p1) - c2 * p2 : (F + c2 * p2) - c1 * p1;
+        R t = plain_upd<E>(F, c1, c2, p1, p2);
         const unsigned am = __activemask();
         if (__any_sync(am, on1 || on2)) {
           T* aux = static_cast<T*>(g.aux[C]);
@@ -204,7 +227,7 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
   }
   if (kind == GMES_KIND_DIELECTRIC) {
     const R c1 = P::cfg(&(cc.c1)), c2 = P::cfg(&(cc.c2));
-    P::st(fp, E ? (F + c1 * p1) - c2 * p2 : (F + c2 * p2) - c1 * p1);
+    P::st(fp, plain_upd<E>(F, c1, c2, p1, p2));
     return;
   }
   T* aux = static_cast<T*>(g.aux[C]);
@@ -218,7 +241,7 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
     if (!on1 && !on2) {
       // outside both slabs kappa = 1 and psi = 0: the dielectric update
       const R c1 = P::cfg(&cc.c1), c2 = P::cfg(&cc.c2);
-      P::st(fp, E ? (F + c1 * p1) - c2 * p2 : (F + c2 * p2) - c1 * p1);
+      P::st(fp, plain_upd<E>(F, c1, c2, p1, p2));
       return;
     }
     R psi1 = pre.a, psi2 = pre.b;
@@ -654,12 +677,112 @@ __device__ __forceinline__ void cell_body(const GridDev& g, int i, int j, int k)
   }
 }
 
-// The register budget of MinBlocks (blocks of 256 threads) in blocks of
-// kCellThreads.
-template <class P>
-struct CellMinBlocks {
-  static constexpr int value = MinBlocks<P>::value * 256 / kCellThreads;
-};
+// The half-step update of one cell in the fast precisions.  Every field
+// value and class id the cell reads is loaded first, so that no load waits
+// for another.  Then a warp whose cells all carry the same class triple, each
+// class of kind DIELECTRIC (one vote, __match_all_sync, and three
+// warp-uniform kind look-ups), updates its three points with those classes'
+// coefficients and nothing else; every other warp goes through the
+// per-point path (update_fast), whose dielectric branch is the same
+// arithmetic, so the two paths agree bit for bit.  The offsets come from
+// the three array-shape families (fst): an active component's strides are
+// its family's.  Measured on GB300 (256^3 cube / 192^3 dispersive scene,
+// Gcell/s, per-point path only -> with the warp-uniform path):
+//   cube FP64 17.42 -> 18.60, FP32 34.17 -> 34.91, df64 21.89 -> 23.63;
+//   dispersive FP64 9.85 -> 10.09, FP32 20.48 -> 22.36, df64 14.85 -> 15.04.
+// A per-warp table of plain warps built at set-up (read with the field
+// values, class maps read only by the other warps) ran slower: cube FP64
+// 18.20, FP32 31.90, df64 22.95.
+template <class P, int SIDE, bool DISP, int MASK, class I>
+__device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, int k) {
+  using R = typename P::R;
+  using T = typename P::T;
+  constexpr int c0 = 3 * SIDE;
+  const I X0 = (I)g.fst[0][0], X1 = (I)g.fst[0][1];
+  const I Y0 = (I)g.fst[1][0], Y1 = (I)g.fst[1][1];
+  const I Z0 = (I)g.fst[2][0], Z1 = (I)g.fst[2][1];
+  const I ii = (I)i, jj = (I)j, kk = (I)k;
+  const I oX = ii * X0 + jj * X1 + kk;
+  const I oY = ii * Y0 + jj * Y1 + kk;
+  const I oZ = ii * Z0 + jj * Z1 + kk;
+  // own points: E (i, j, k); Hx[i, j+1, k+1], Hy[i+1, j, k+1], Hz[i+1, j+1, k]
+  const I l0 = SIDE == 0 ? oX : oX + X1 + 1;
+  const I l1 = SIDE == 0 ? oY : oY + Y0 + 1;
+  const I l2 = SIDE == 0 ? oZ : oZ + Z0 + Z1;
+  const R f0 = ldf<P, MASK, c0>(g, l0), f1 = ldf<P, MASK, c0 + 1>(g, l1),
+          f2 = ldf<P, MASK, c0 + 2>(g, l2);
+  R d01, d02, d11, d12, d21, d22;  // (D1, D2) of each component
+  if constexpr (SIDE == 0) {
+    const R hz_a = ldf<P, MASK, 5>(g, oZ + Z0 + Z1);  // Hz[i+1, j+1, k]
+    const R hz_b = ldf<P, MASK, 5>(g, oZ + Z0);       // Hz[i+1, j,   k]
+    const R hz_c = ldf<P, MASK, 5>(g, oZ + Z1);       // Hz[i,   j+1, k]
+    const R hy_a = ldf<P, MASK, 4>(g, oY + Y0 + 1);   // Hy[i+1, j, k+1]
+    const R hy_b = ldf<P, MASK, 4>(g, oY + Y0);       // Hy[i+1, j, k]
+    const R hy_c = ldf<P, MASK, 4>(g, oY + 1);        // Hy[i,   j, k+1]
+    const R hx_a = ldf<P, MASK, 3>(g, oX + X1 + 1);   // Hx[i, j+1, k+1]
+    const R hx_b = ldf<P, MASK, 3>(g, oX + X1);       // Hx[i, j+1, k]
+    const R hx_c = ldf<P, MASK, 3>(g, oX + 1);        // Hx[i, j,   k+1]
+    d01 = hz_a - hz_b; d02 = hy_a - hy_b;
+    d11 = hx_a - hx_b; d12 = hz_a - hz_c;
+    d21 = hy_a - hy_c; d22 = hx_a - hx_c;
+  } else {
+    const R ez_0 = ldf<P, MASK, 2>(g, oZ);       // Ez[i, j, k]
+    const R ez_j = ldf<P, MASK, 2>(g, oZ + Z1);  // Ez[i, j+1, k]
+    const R ez_i = ldf<P, MASK, 2>(g, oZ + Z0);  // Ez[i+1, j, k]
+    const R ey_0 = ldf<P, MASK, 1>(g, oY);       // Ey[i, j, k]
+    const R ey_k = ldf<P, MASK, 1>(g, oY + 1);   // Ey[i, j, k+1]
+    const R ey_i = ldf<P, MASK, 1>(g, oY + Y0);  // Ey[i+1, j, k]
+    const R ex_0 = ldf<P, MASK, 0>(g, oX);       // Ex[i, j, k]
+    const R ex_k = ldf<P, MASK, 0>(g, oX + 1);   // Ex[i, j, k+1]
+    const R ex_j = ldf<P, MASK, 0>(g, oX + X1);  // Ex[i, j+1, k]
+    d01 = ez_j - ez_0; d02 = ey_k - ey_0;
+    d11 = ex_k - ex_0; d12 = ez_i - ez_0;
+    d21 = ey_i - ey_0; d22 = ex_j - ex_0;
+  }
+  const uint8_t id0 = ldc<MASK, c0>(g, l0), id1 = ldc<MASK, c0 + 1>(g, l1),
+                id2 = ldc<MASK, c0 + 2>(g, l2);
+  const uint32_t t = (uint32_t)id0 | (uint32_t)id1 << 8 | (uint32_t)id2 << 16;
+  int same = 0;
+  __match_all_sync(__activemask(), t, &same);
+  const bool fast =
+      same && !g.pointwise &&
+      (!is_active<MASK, c0>(g) || g.tab[c0][id0].kind == GMES_KIND_DIELECTRIC) &&
+      (!is_active<MASK, c0 + 1>(g) || g.tab[c0 + 1][id1].kind == GMES_KIND_DIELECTRIC) &&
+      (!is_active<MASK, c0 + 2>(g) || g.tab[c0 + 2][id2].kind == GMES_KIND_DIELECTRIC);
+  constexpr bool E = SIDE == 0;
+  if (fast) {  // warp-uniform
+    const ClassCoef& qa = g.tab[c0][id0];
+    const ClassCoef& qb = g.tab[c0 + 1][id1];
+    const ClassCoef& qc = g.tab[c0 + 2][id2];
+    if (is_active<MASK, c0>(g))
+      P::st(static_cast<T*>(g.f[c0]) + l0,
+            plain_upd<E>(f0, P::cfg(&qa.c1), P::cfg(&qa.c2), d01, d02));
+    if (is_active<MASK, c0 + 1>(g))
+      P::st(static_cast<T*>(g.f[c0 + 1]) + l1,
+            plain_upd<E>(f1, P::cfg(&qb.c1), P::cfg(&qb.c2), d11, d12));
+    if (is_active<MASK, c0 + 2>(g))
+      P::st(static_cast<T*>(g.f[c0 + 2]) + l2,
+            plain_upd<E>(f2, P::cfg(&qc.c1), P::cfg(&qc.c2), d21, d22));
+    return;
+  }
+  if constexpr (SIDE == 0) {
+    const int xc[3] = {i, j, k};
+    const Pre<P> pa = pre_of<P, MASK, 0, false>(g, l0, xc, id0);
+    const Pre<P> pb = pre_of<P, MASK, 1, false>(g, l1, xc, id1);
+    const Pre<P> pc = pre_of<P, MASK, 2, false>(g, l2, xc, id2);
+    upd<P, MASK, 0, false, DISP>(g, l0, xc, d01, d02, f0, id0, pa);
+    upd<P, MASK, 1, false, DISP>(g, l1, xc, d11, d12, f1, id1, pb);
+    upd<P, MASK, 2, false, DISP>(g, l2, xc, d21, d22, f2, id2, pc);
+  } else {
+    const int x3[3] = {i, j + 1, k + 1}, x4[3] = {i + 1, j, k + 1}, x5[3] = {i + 1, j + 1, k};
+    const Pre<P> pa = pre_of<P, MASK, 3, false>(g, l0, x3, id0);
+    const Pre<P> pb = pre_of<P, MASK, 4, false>(g, l1, x4, id1);
+    const Pre<P> pc = pre_of<P, MASK, 5, false>(g, l2, x5, id2);
+    upd<P, MASK, 3, false, false>(g, l0, x3, d01, d02, f0, id0, pa);
+    upd<P, MASK, 4, false, false>(g, l1, x4, d11, d12, f1, id1, pb);
+    upd<P, MASK, 5, false, false>(g, l2, x5, d21, d22, f2, id2, pc);
+  }
+}
 
 template <class P, int SIDE, bool STRICT, bool DISP, int MASK, class I>
 __global__ void __launch_bounds__(kCellThreads, CellMinBlocks<P>::value)
@@ -671,7 +794,10 @@ __global__ void __launch_bounds__(kCellThreads, CellMinBlocks<P>::value)
   const int j = blockIdx.y * (kCellThreads >> bx_log2) + ty;
   const int i = i0 + (int)blockIdx.z;
   if (k >= g.n[2] || j >= g.n[1] || i >= g.n[0]) return;
-  cell_body<P, SIDE, STRICT, DISP, MASK, I>(g, i, j, k);
+  if constexpr (STRICT)
+    cell_body<P, SIDE, STRICT, DISP, MASK, I>(g, i, j, k);
+  else
+    cell_body_fast<P, SIDE, DISP, MASK, I>(g, i, j, k);
 }
 
 // Cells per block row along k (log2): a warp covers 16 cells of two rows
@@ -687,8 +813,8 @@ __global__ void __launch_bounds__(kCellThreads, CellMinBlocks<P>::value)
 //                                    FP32 19.34 / 20.08 / 18.47
 //                                    df64 12.73 / 13.86 / 13.80
 // (FP64 E half of the cube: 14.4 -> 13.7 FP64 warp-instructions per cell,
-// what a warp-level count of the slabs predicts for both shapes.)
-constexpr int kRowLog2 = 4;
+// what a warp-level count of the slabs predicts for both shapes.)  The row
+// length is kRowLog2 (cell_tiling).
 
 template <class P, bool STRICT, int MASK, class I>
 void launch_cell(const GridDev& d, int side, bool disp, dim3 grid, int bx_log2, int i0,
@@ -923,12 +1049,18 @@ static_assert(sizeof(GridDev) % 16 == 0, "GridDev is copied as 16-byte words");
 // the single-grid kernel, whose descriptor is a kernel parameter; from
 // shared memory it runs 1.3x slower (measured on GB300, 160^3 cube).
 template <class P, int SIDE, bool STRICT, bool DISP>
-__global__ void __launch_bounds__(kThreads, MinBlocks<P>::value)
+__global__ void __launch_bounds__(kBatchThreads, CellMinBlocks<P>::value)
     k_multi_cell(const BatchView v, int s) {
   __shared__ __align__(16) unsigned char desc[sizeof(GridDev)];
   const GridDev& g = *reinterpret_cast<const GridDev*>(desc);
   int cached = -1;
-  for (int64_t b = blockIdx.x; b < v.tiles; b += gridDim.x) {
+  // a persistent grid (fewer blocks than tiles) gives each block a
+  // contiguous range of tiles, so that a block mostly stays on one grid and
+  // copies its descriptor once
+  const int64_t per = (v.tiles + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = (int64_t)blockIdx.x * per;
+  const int64_t b1 = b0 + per < v.tiles ? b0 + per : v.tiles;
+  for (int64_t b = b0; b < b1; ++b) {
     const int job = find_job<int64_t>(v.tile_prefix, v.njobs, b);  // block-uniform
     if (s >= __ldg(v.steps + job)) continue;
     if (job != cached) {
@@ -941,7 +1073,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<P>::value)
       cached = job;
     }
     const int bxl = __ldg(v.bxl + job);
-    const int bx = 1 << bxl, by = kThreads >> bxl;
+    const int bx = 1 << bxl, by = kBatchThreads >> bxl;
     const int nkb = (g.n[2] + bx - 1) / bx, njb = (g.n[1] + by - 1) / by;
     const int64_t local = b - __ldg(v.tile_prefix + job);
     const int i = (int)(local / ((int64_t)nkb * njb));
@@ -951,7 +1083,12 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<P>::value)
     const int j = jb * by + (threadIdx.x >> bxl);
     // batched grids hold fewer than 2^31 points per component (checked when
     // the batch is prepared)
-    if (k < g.n[2] && j < g.n[1]) cell_body<P, SIDE, STRICT, DISP, 0, int32_t>(g, i, j, k);
+    if (k < g.n[2] && j < g.n[1]) {
+      if constexpr (STRICT)
+        cell_body<P, SIDE, STRICT, DISP, 0, int32_t>(g, i, j, k);
+      else
+        cell_body_fast<P, SIDE, DISP, 0, int32_t>(g, i, j, k);
+    }
   }
 }
 
@@ -1003,9 +1140,8 @@ void run_half(const Plan& p, int side, int st, cudaStream_t s) {
     k_ghost_c<STRICT><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
   else
     k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
-  int bx_log2 = 0;
-  while (bx_log2 < kRowLog2 && (1 << bx_log2) < d.n[2]) ++bx_log2;
-  const int bx = 1 << bx_log2, by = kCellThreads / bx;
+  const CellTiling tl = cell_tiling(d.n);
+  const int bx_log2 = tl.bx_log2, bx = tl.bx, by = tl.by;
   const int nplanes = p.cplx ? 2 : 1;
   for (int part = 0; part < nplanes; ++part) {
     const GridDev& v = part == 0 ? p.re : p.im;
@@ -1072,11 +1208,11 @@ cudaError_t run_batch(const BatchView& v, bool disp, int nsteps, int blocks, cud
       if (cells > 0) {
         if (side == 0) {
           if (disp)
-            k_multi_cell<P, 0, STRICT, true><<<cells, kThreads, 0, st>>>(v, s);
+            k_multi_cell<P, 0, STRICT, true><<<cells, kBatchThreads, 0, st>>>(v, s);
           else
-            k_multi_cell<P, 0, STRICT, false><<<cells, kThreads, 0, st>>>(v, s);
+            k_multi_cell<P, 0, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s);
         } else {
-          k_multi_cell<P, 1, STRICT, false><<<cells, kThreads, 0, st>>>(v, s);
+          k_multi_cell<P, 1, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s);
         }
       }
       if (sblocks > 0) k_multi_sources<P, STRICT><<<sblocks, 128, 0, st>>>(v, side, s);
@@ -1099,6 +1235,53 @@ cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nstep
     default:
       return cudaErrorInvalidValue;
   }
+}
+
+// Non-finite guard (gmes_nonfinite): an infinity or NaN has an all-ones
+// exponent; the test is on the bits, so no floating-point pipe is used.
+__device__ __forceinline__ bool nonfinite(double v) {
+  return ((__double_as_longlong(v) >> 52) & 0x7ff) == 0x7ff;
+}
+__device__ __forceinline__ bool nonfinite(float v) {
+  return ((__float_as_uint(v) >> 23) & 0xff) == 0xff;
+}
+__device__ __forceinline__ bool nonfinite(float2 v) { return nonfinite(v.x); }  // hi word
+
+template <class T>
+__global__ void k_nonfinite(const GridDev g, int planes, int32_t* flag) {
+  bool bad = false;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int c = 0; c < 6; ++c) {
+    if (!((g.active >> c) & 1)) continue;
+    const T* f = static_cast<const T*>(g.f[c]);
+    const int64_t n = g.npts[c] * planes;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride)
+      bad = bad || nonfinite(f[t]);
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *flag = 1;
+}
+
+cudaError_t launch_nonfinite(const gmes_grid_desc& g, const GridDev& d, int32_t* flag,
+                             cudaStream_t s) {
+  const int planes = (g.flags & GMES_FLAG_COMPLEX) ? 2 : 1;
+  int64_t most = 1;
+  for (int c = 0; c < 6; ++c) most = d.npts[c] * planes > most ? d.npts[c] * planes : most;
+  const int blocks = (int)((most + 255) / 256 < 152 * 8 ? (most + 255) / 256 : 152 * 8);
+  switch (g.precision) {
+    case GMES_FP64:
+    case GMES_FP64_STRICT:
+      k_nonfinite<double><<<blocks, 256, 0, s>>>(d, planes, flag);
+      break;
+    case GMES_FP32:
+      k_nonfinite<float><<<blocks, 256, 0, s>>>(d, planes, flag);
+      break;
+    case GMES_DF64:
+      k_nonfinite<float2><<<blocks, 256, 0, s>>>(d, planes, flag);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_step(const gmes_grid_desc& g, const Plan& p, int nsteps, cudaStream_t s) {

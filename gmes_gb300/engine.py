@@ -481,5 +481,13 @@ class GridEngine:
             return a.view(torch.float32).view((na,) + shape)
         return a.view(torch.float32).view((na,) + shape + (2,))
 
+    def check_finite(self, flag_ptr, stream=None):
+        """Enqueue the non-finite guard (gmes_nonfinite): sets the int32 at
+        device address ``flag_ptr`` to 1 when any field value is an infinity
+        or a NaN.  On ``stream`` (a cudaStream_t handle) or the engine's."""
+        st = self.stream if stream is None else stream
+        N.check(self.lib.gmes_nonfinite(C.byref(self.desc), C.c_void_p(flag_ptr),
+                                        C.c_void_p(st)))
+
     def synchronize(self):
         self._stream.synchronize()

@@ -10,12 +10,18 @@ replayed as a CUDA graph).  Between chunks it
   them (the grid's buffer sizes from ``gmes_grid_sizes`` against
   ``torch.cuda.mem_get_info`` minus a reserve, and an optional budget) and
   a slot is free;
-* compiles the next jobs' scenes on the host while the chunk runs.
+* compiles the next jobs' scenes on the host while the chunk runs;
+* fails, alone, every resident job whose fields went non-finite during the
+  chunk (a device check after each chunk, ``gmes_nonfinite``), and every
+  job cancelled with ``cancel(jid)``, queued or resident.
 
 A job's arithmetic does not depend on which other grids share its chunks,
 so its result is the same alone and in the mix.  Latency of a job =
 completion time - arrival time; the report gives p50 / p99 and the
-aggregate cell-updates per second.
+aggregate cell-updates per second.  Failures surface to the caller as the
+job's ``error`` text and touch no other job, as the reference's binding
+turns a failed update into an exception for its caller
+(src/cpp23_support.hh:155-173, src/pw_material.i:23-33).
 """
 
 import time
@@ -74,11 +80,13 @@ class Server:
     hold fewer cells than this with it (one job is always admitted; 0: no
     limit).  A few million cells fill the GPU, so beyond that more resident
     grids only share it: every job's latency grows and throughput does not.
+    ``guard``: check every resident grid for non-finite field values after
+    each chunk and fail the jobs that have them.
     """
 
     def __init__(self, precision="fp64", chunk=64, max_slots=64, memory_budget=None,
                  reserve=2 << 30, tuner=None, use_graphs=True, device=None,
-                 fill_cells=FILL_CELLS):
+                 fill_cells=FILL_CELLS, guard=True):
         torch = _torch()
         self.precision = precision
         self.chunk = int(chunk)
@@ -104,6 +112,59 @@ class Server:
         self.fill_cells = int(fill_cells)
         self.resident_cells = 0
         self.max_resident = 0
+        self.guard = bool(guard)
+        self._flags = torch.zeros(self.max_slots, dtype=torch.int32, device=self.device)
+        self._flags_host = torch.zeros(self.max_slots, dtype=torch.int32).pin_memory()
+        self._cancel = set()
+
+    # -- failures ------------------------------------------------------------
+    def cancel(self, jid):
+        """Cancel job ``jid``: a queued job never starts, a resident one stops
+        at the end of its current chunk; either is reported as failed with
+        the error "cancelled".  Safe to call from another thread or from the
+        ``on_chunk`` callback of ``run``."""
+        self._cancel.add(jid)
+
+    def _fail(self, job, now, error):
+        """Take a job out of service with ``error``, freeing what it holds."""
+        job.error = error
+        job.t_finish = now
+        if job.engine is not None:
+            job.engine = None
+            self.used_bytes -= job.bytes
+            self.resident_cells -= job.cells
+        self.failed.append(job)
+
+    def _apply_cancellations(self, pending, waiting, now):
+        """Remove cancelled jobs from the arrival list, the queue and the
+        resident set (between chunks)."""
+        if not self._cancel:
+            return
+        hit = self._cancel
+        for lst in (pending, waiting):
+            for job in [j for j in lst if j.jid in hit]:
+                lst.remove(job)
+                self._fail(job, now, "cancelled")
+        for job in [j for j in self.resident if j.jid in hit]:
+            self.resident.remove(job)
+            self._fail(job, now, "cancelled")
+        self._cancel = set()
+
+    def _enqueue_guard(self, jobs):
+        """After a chunk: the non-finite check of every resident grid, its
+        flags copied to pinned host memory on the server's stream."""
+        n = len(jobs)
+        with _torch().cuda.stream(self.stream):
+            self._flags[:n].zero_()
+            base = self._flags.data_ptr()
+            for q, job in enumerate(jobs):
+                job.engine.check_finite(base + 4 * q, self.stream.cuda_stream)
+            self._flags_host[:n].copy_(self._flags[:n], non_blocking=True)
+
+    def _diverged(self, jobs):
+        """The jobs whose check found a non-finite value (after the chunk's
+        synchronisation)."""
+        return [j for j, f in zip(jobs, self._flags_host[:len(jobs)].tolist()) if f]
 
     # -- admission ---------------------------------------------------------
     @staticmethod
@@ -188,12 +249,13 @@ class Server:
             self._batch_key = key
         return self._batch
 
-    def run(self, jobs, realtime=True):
+    def run(self, jobs, realtime=True, on_chunk=None):
         """Serve ``jobs`` (arrival times relative to the start); return the report.
 
         With ``realtime`` the server waits for arrivals on the wall clock;
         otherwise a job is available as soon as the clock reaches its
-        arrival or the server is idle.
+        arrival or the server is idle.  ``on_chunk(server)`` is called after
+        every chunk (for example to cancel jobs).
         """
         torch = _torch()
         pending = sorted(jobs)
@@ -202,6 +264,7 @@ class Server:
         cell_updates = 0
         while pending or waiting or self.resident:
             now = time.perf_counter() - t0
+            self._apply_cancellations(pending, waiting, now)
             while pending and (pending[0].arrival <= now or
                                (not realtime and not self.resident and not waiting)):
                 waiting.append(pending.pop(0))
@@ -231,6 +294,11 @@ class Server:
             if self.tuner is not None:
                 self.tuner.observe_start(batch)
             self.launches += batch.run(steps, n0s)
+            if self.tuner is not None:
+                self.tuner.observe_stop(batch)
+            if self.guard:
+                self._enqueue_guard(self.resident)
+                self.launches += len(self.resident)
             # host work overlaps the chunk: compile the next arrivals' scenes
             for job in waiting[:4]:
                 self._compile(job)
@@ -239,15 +307,22 @@ class Server:
                 self.tuner.observe_end(batch, sum(s * j.cells for s, j in zip(steps, self.resident)))
             self.chunks += 1
             now = time.perf_counter() - t0
+            bad = set(id(j) for j in self._diverged(self.resident)) if self.guard else set()
             still = []
             for j, s in zip(self.resident, steps):
                 j.done += s
                 cell_updates += s * j.cells
-                if j.done >= j.nsteps:
+                if id(j) in bad:
+                    self._fail(j, now, f"non-finite field values (Inf or NaN) by step {j.done}: "
+                                       "the simulation diverged, e.g. a time step above the "
+                                       "Courant stability limit")
+                elif j.done >= j.nsteps:
                     self._retire(j, now)
                 else:
                     still.append(j)
             self.resident = still
+            if on_chunk is not None:
+                on_chunk(self)
         torch.cuda.synchronize(self.device)
         wall = time.perf_counter() - t0
         return self.report(wall, cell_updates)
@@ -269,16 +344,19 @@ def run_one_at_a_time(jobs, precision="fp64", device=None, realtime=False):
     """The same jobs, each run alone with the plain single-grid kernels, in
     arrival order.  With ``realtime`` a job starts no earlier than its
     arrival (as in ``Server.run``), so throughput and latencies compare
-    with the batched server on the same arrival process."""
+    with the batched server on the same arrival process.  ``job_s`` holds
+    each job's own wall time (scene, set-up and steps), in arrival order."""
     torch = _torch()
     t0 = time.perf_counter()
     cell_updates = 0
     lat = []
+    job_s = []
     for job in sorted(jobs):
         if realtime:
             wait = job.arrival - (time.perf_counter() - t0)
             if wait > 0:
                 time.sleep(wait)
+        tj = time.perf_counter()
         sim = job.build()
         scene = sim.compile()
         eng = GridEngine(scene, precision=precision, device=device, use_graphs=False)
@@ -288,6 +366,7 @@ def run_one_at_a_time(jobs, precision="fp64", device=None, realtime=False):
         if job.keep_fields:
             job.fields = [eng.read(c) for c in range(6)]
         del eng
+        job_s.append(time.perf_counter() - tj)
         lat.append(time.perf_counter() - t0 - job.arrival)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -295,4 +374,61 @@ def run_one_at_a_time(jobs, precision="fp64", device=None, realtime=False):
     return {"wall_s": wall, "cell_updates": cell_updates,
             "gcells_per_s": cell_updates / wall / 1e9,
             "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
-            "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None}
+            "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "job_s": job_s}
+
+
+def saturated_step_seconds(scene, precision="fp64", min_cells=1 << 21, max_copies=128,
+                           steps=24, device=None):
+    """Seconds per step of one grid when copies of it fill the GPU.
+
+    ``copies`` = min(max_copies, ceil(min_cells / cells)) grids of ``scene``
+    advance together through ``Batch`` (one multi-grid launch per kernel
+    kind and half-step; a grid of SOLO_CELLS cells or more runs its own
+    single-grid kernels, which fill the GPU by themselves); the device time
+    of ``steps`` steps (CUDA events, after a warm-up chunk) divided by
+    copies x steps is the grid's step time at a saturated GPU -- the least
+    time any batching of it can give.  Returns (seconds, copies).
+    """
+    torch = _torch()
+    cells = scene.cells
+    copies = int(max(1, min(max_copies, -(-min_cells // max(cells, 1)))))
+    engines = [GridEngine(scene, precision=precision, device=device, src_chunk=steps)
+               for _ in range(copies)]
+    batch = Batch(engines)
+    batch.run([steps] * copies, [0.0] * copies)  # warm-up: loads kernels, captures graphs
+    batch.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(batch.stream)
+    batch.run([steps] * copies, [float(steps)] * copies)
+    t1.record(batch.stream)
+    batch.synchronize()
+    sec = t0.elapsed_time(t1) / 1e3 / (copies * steps)
+    del batch, engines
+    return sec, copies
+
+
+def batching_bound(jobs, job_s, precision="fp64", device=None, cache=None):
+    """The largest speed-up over one-at-a-time any batching can give on ``jobs``.
+
+    ``job_s``: each job's one-at-a-time wall time (``run_one_at_a_time``),
+    in arrival order.  Every job's least GPU time is its steps x its
+    saturated step time (``saturated_step_seconds``); the bound is the
+    summed one-at-a-time time over the summed least time.  ``cache`` (a
+    dict) reuses measurements of identical grids.
+    """
+    cache = {} if cache is None else cache
+    least = 0.0
+    per_job = []
+    for job in sorted(jobs):
+        scene = job.build().compile()
+        key = (tuple(scene.n), scene.cells, len(scene.classes[0]), scene.dispersive,
+               tuple(len(scene.classes[c]) for c in range(6)), repr(scene.dt))
+        if key not in cache:
+            cache[key] = saturated_step_seconds(scene, precision, device=device)
+        sec, copies = cache[key]
+        least += sec * job.nsteps
+        per_job.append((scene.cells, job.nsteps, sec, copies))
+    total = float(sum(job_s))
+    return {"bound": total / least if least > 0 else None, "one_at_a_time_s": total,
+            "saturated_s": least, "per_job": per_job}

@@ -46,7 +46,7 @@
 extern "C" {
 #endif
 
-#define GMES_ABI_VERSION 5
+#define GMES_ABI_VERSION 6
 #define GMES_MAX_CLASSES 256 /* class ids are u8 */
 #define GMES_MAX_PML 4       /* PML materials per grid */
 #define GMES_MAX_POLES 8     /* Drude/Lorentz poles, DCP terms per class */
@@ -89,6 +89,12 @@ typedef enum {
    couple only through the Bloch phases of the ghost copies.  FP64 and
    FP64_STRICT only. */
 #define GMES_FLAG_COMPLEX 2
+/* Every warp of the cell kernels takes the per-point path.  By default a
+   warp whose points all carry the same dielectric class per component
+   updates them without the per-point kind look-ups and branches; the
+   arithmetic is the same, so the fields are bit-identical either way (a
+   switch for tests and measurements).  No counterpart in the reference. */
+#define GMES_FLAG_POINTWISE 4
 
 /* Field components: bit c of gmes_grid_desc.active. */
 enum { GMES_EX = 0, GMES_EY = 1, GMES_EZ = 2, GMES_HX = 3, GMES_HY = 4, GMES_HZ = 5 };
@@ -276,6 +282,18 @@ gmes_status gmes_set_pml_profile(const gmes_grid_desc* g, int32_t pml, int32_t c
  */
 gmes_status gmes_get_pml_profile(const gmes_grid_desc* g, int32_t pml, int32_t comp,
                                  int32_t axis, double* out, void* stream);
+
+/*
+ * Non-finite guard: sets *flag (an int32 in DEVICE memory) to 1 when any
+ * field value of the grid (both planes of a complex grid) is an infinity or
+ * a NaN, as a simulation past its stability limit produces; it never clears
+ * the flag.  The reference has no device state to watch: a failure in its
+ * binding surfaces to the caller as an exception and leaves everything else
+ * untouched (src/cpp23_support.hh:155-173, src/pw_material.i:23-33).  A
+ * server reads the flag between chunks and fails that job alone.
+ * Asynchronous on `stream`.
+ */
+gmes_status gmes_nonfinite(const gmes_grid_desc* g, int32_t* flag, void* stream);
 
 /* Zero every field and state buffer (FDTD.init's zero fields). */
 gmes_status gmes_reset(const gmes_grid_desc* g, void* stream);

@@ -147,3 +147,52 @@ def test_one_at_a_time_baseline_runs():
     rep = run_one_at_a_time(jobs)
     assert rep["cell_updates"] > 0 and rep["gcells_per_s"] > 0
     assert rep["latency_p99_s"] >= rep["latency_p50_s"] > 0
+
+
+def unstable():
+    """A TMz grid stepped at 1.5 times the Courant limit: its fields grow
+    until they overflow to Inf (no fault: IEEE arithmetic)."""
+    space = G.Cartesian(size=(3, 3, 0), resolution=10)
+    geom = [G.DefaultMedium(material=G.Dielectric()), G.Shell(material=G.Cpml(), thickness=0.5)]
+    src = [G.PointSource(src_time=G.Bandpass(freq=0.8, fwidth=1.0), center=(0, 0, 0),
+                         component=G.Ez)]
+    return G.TMzFDTD(space, geom, src, courant_ratio=1.5, verbose=False)
+
+
+def test_server_fails_a_diverging_job_alone():
+    builds = mix()[:4]
+    jobs = [Job(arrival=0.0, jid=i, build=b, nsteps=n, keep_fields=True)
+            for i, (b, n) in enumerate(builds)]
+    jobs.append(Job(arrival=0.0, jid=77, build=unstable, nsteps=1500))
+    server = Server(precision="fp64", chunk=16, fill_cells=0)
+    rep = server.run(jobs, realtime=False)
+    assert rep["jobs"] == len(builds) and rep["failed"] == 1
+    bad = server.failed[0]
+    assert bad.jid == 77 and "non-finite" in bad.error and bad.done < 1500
+    assert server.used_bytes == 0 and server.resident_cells == 0
+    for job in server.finished:
+        b, n = builds[job.jid]
+        ref = alone(b, n, "fp64")
+        for c in range(6):
+            assert np.array_equal(job.fields[c], ref[c]), (job.jid, c)
+
+
+def test_server_cancels_a_resident_job():
+    builds = mix()[:3]
+    jobs = [Job(arrival=0.0, jid=i, build=b, nsteps=n, keep_fields=True)
+            for i, (b, n) in enumerate(builds)]
+    jobs.append(Job(arrival=0.0, jid=5, build=builds[0][0], nsteps=5000))
+    server = Server(precision="fp64", chunk=16, fill_cells=0)
+
+    def on_chunk(srv):
+        if srv.chunks == 2:
+            srv.cancel(5)
+    rep = server.run(jobs, realtime=False, on_chunk=on_chunk)
+    assert rep["jobs"] == 3 and rep["failed"] == 1
+    assert server.failed[0].jid == 5 and server.failed[0].error == "cancelled"
+    assert server.failed[0].done == 32
+    for job in server.finished:
+        b, n = builds[job.jid]
+        ref = alone(b, n, "fp64")
+        for c in range(6):
+            assert np.array_equal(job.fields[c], ref[c]), (job.jid, c)

@@ -69,3 +69,34 @@ def test_no_fill_limit_and_the_other_limits(monkeypatch):
     srv.memory_budget = 1200
     assert srv._admit(jobs[2], 0.0) == "admitted"
     assert srv.resident_cells == 1200 and srv.max_resident == 3
+
+
+def test_cancel_removes_queued_and_resident_jobs(monkeypatch):
+    srv = _server(monkeypatch, fill_cells=0)
+    srv._cancel = set()
+    a, b, c, d = _job(0, 100), _job(1, 200), _job(2, 300), _job(3, 400)
+    assert srv._admit(a, 0.0) == "admitted" and srv._admit(b, 0.0) == "admitted"
+    pending, waiting = [d], [c]
+    srv.cancel(1)   # resident
+    srv.cancel(2)   # queued
+    srv.cancel(3)   # not yet arrived
+    srv.cancel(42)  # unknown: ignored
+    srv._apply_cancellations(pending, waiting, 2.0)
+    assert pending == [] and waiting == [] and srv.resident == [a]
+    assert sorted(j.jid for j in srv.failed) == [1, 2, 3]
+    assert all(j.error == "cancelled" and j.t_finish == 2.0 for j in srv.failed)
+    assert srv.used_bytes == 100 and srv.resident_cells == 100
+    assert b.engine is None
+    srv._apply_cancellations(pending, waiting, 3.0)  # nothing left to cancel
+    assert len(srv.failed) == 3
+
+
+def test_failed_resident_job_frees_its_share(monkeypatch):
+    srv = _server(monkeypatch, fill_cells=0)
+    a, b = _job(0, 100), _job(1, 250)
+    srv._admit(a, 0.0)
+    srv._admit(b, 0.0)
+    srv.resident.remove(b)
+    srv._fail(b, 1.5, "non-finite field values")
+    assert srv.used_bytes == 100 and srv.resident_cells == 100
+    assert srv.failed == [b] and b.t_finish == 1.5 and b.engine is None
