@@ -675,7 +675,8 @@ def design_launches(prob, precision, block_steps, max_block_steps=4):
     One step per launch: E, E sources, H, H sources per step of every pass.
     FP32 temporally blocked (block_steps 0 = the library's most, 4): the
     forward takes one launch per block of up to that many steps of each
-    call, the adjoint one per odd block of up to that many steps (1 or 3).
+    call; the adjoint the fewest launches of at most that many steps whose
+    count has the parity of the call's steps (the library's adj_launches).
     Passes: forward and adjoint over all steps when the forward records the
     history; forward, recompute and adjoint per checkpoint segment otherwise.
     """
@@ -688,13 +689,10 @@ def design_launches(prob, precision, block_steps, max_block_steps=4):
         return 4 * passes * nsteps
 
     def adj(k):
-        n = 0
-        while k > 0:
-            m = min(k, per)
-            m -= 1 - m % 2
-            k -= m
+        n = (k + per - 1) // per
+        if n % 2 != k % 2:
             n += 1
-        return n
+        return min(n, k)
     fwd = sum((k + per - 1) // per for k in calls)
     return fwd * (passes - 1) + sum(adj(k) for k in calls)
 

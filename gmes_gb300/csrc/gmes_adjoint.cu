@@ -822,13 +822,13 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
 // Adjoint steps n0 + nsub down to n0 + 1 of one tile (the transposes of
 // k_tmz_ah / k_tmz_ae, same order), the field adjoints from t.l to
 // t.tmp[0..2]; the gradient of step n uses hist slot n - step0 - 1.  The
-// psi adjoints are read from the buffer step n0 + nsub reads
-// ((n0 + nsub) & 1) and written to the one step n0 + 1 writes, as the
-// one-step kernels do; nsub is odd, so the two buffers differ and no block
-// overwrites what another still reads.
+// psi adjoints are read from buffer rb and written to the other one, so no
+// block overwrites what another still reads (adjoint_blocked chooses rb so
+// that a call leaves them where the one-step kernels' step-parity
+// convention expects them).
 template <int RI>
 __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
-    k_tmz_tb_adj(const GridDev g, const TmzDev t, int n0, int nsub, int step0) {
+    k_tmz_tb_adj(const GridDev g, const TmzDev t, int n0, int nsub, int step0, int rb) {
   using P = PolF32;
   using G = TbGeom<RI>;
   constexpr int H = G::H, RJ = G::RJ, TI = G::TI, TJ = G::TJ, NP = G::NP, Q = G::Q;
@@ -844,7 +844,7 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
   const int j = wrap_index(rj0 + c, t.ny);
   const bool jtile = c >= H && c < H + TJ && rj0 + c < t.ny;
   const int64_t base = (int64_t)b * t.plane;
-  const int rb = (n0 + nsub) & 1, wb = ((n0 + 1) & 1) ^ 1;
+  const int wb = rb ^ 1;
   int li[Q];
   TbPoint pt[Q];
   unsigned fl[Q];
@@ -1115,12 +1115,18 @@ cudaError_t forward_blocked(const GridDev& g, const TmzDev& t, int step0, int ns
   return cudaGetLastError();
 }
 
-// Steps per launch of the blocked adjoint, largest first: odd counts of at
-// most per_launch (see k_tmz_tb_adj).
-int adj_chunk(int remaining, int per_launch) {
-  int m = remaining < per_launch ? remaining : per_launch;
-  if (m % 2 == 0) --m;
-  return m;
+// Launches of the blocked adjoint for nsteps steps of at most per_launch
+// each.  Each launch reads the psi adjoints from one buffer and writes the
+// other; a call starts from the buffer the one-step kernels' step n0 + nsteps
+// reads ((n0 + nsteps) & 1) and must end in the one step n0 + 1 writes
+// (n0 & 1), so the number of launches has the parity of nsteps: the fewest
+// launches of that parity, their step counts as even as possible.  (Odd
+// step counts per launch, the earlier rule, capped launches at 3 steps
+// against the forward's 4.)
+int adj_launches(int nsteps, int per_launch) {
+  int k = (nsteps + per_launch - 1) / per_launch;
+  if ((k & 1) != (nsteps & 1)) ++k;
+  return k < nsteps ? k : nsteps;
 }
 
 cudaError_t adjoint_blocked(const GridDev& g, const TmzDev& t, int step0, int nsteps,
@@ -1130,19 +1136,23 @@ cudaError_t adjoint_blocked(const GridDev& g, const TmzDev& t, int step0, int ns
                                        (int)kTbAdjSmem);
   if (e != cudaSuccess) return e;
   if (t.tmp[0] == nullptr) return cudaErrorInvalidValue;
+  if (nsteps <= 0) return cudaSuccess;
   const dim3 grid = tb_grid<kTbAdjRI>(t), block(kTbRJ, kTbRows);
-  int launches = 0;
-  for (int hi = nsteps; hi > 0; hi -= adj_chunk(hi, per_launch)) ++launches;
+  const int launches = adj_launches(nsteps, per_launch);
   TmzDev u = t;
   if (launches % 2 == 1) {
     e = copy_state(t.tmp, t.l, 3, (int64_t)t.nb * t.plane * (int64_t)sizeof(float), s);
     if (e != cudaSuccess) return e;
     swap_adjoints(u);
   }
-  for (int hi = nsteps; hi > 0;) {
-    const int m = adj_chunk(hi, per_launch);
-    k_tmz_tb_adj<kTbAdjRI><<<grid, block, kTbAdjSmem, s>>>(g, u, step0 + hi - m, m, step0);
+  int rb = (step0 + nsteps) & 1;
+  int hi = nsteps;
+  for (int q = 0; q < launches; ++q) {
+    // launch q takes an even share of the steps left
+    const int m = (hi + (launches - q) - 1) / (launches - q);
+    k_tmz_tb_adj<kTbAdjRI><<<grid, block, kTbAdjSmem, s>>>(g, u, step0 + hi - m, m, step0, rb);
     swap_adjoints(u);
+    rb ^= 1;
     hi -= m;
   }
   return cudaGetLastError();

@@ -218,6 +218,38 @@ BatchView batch_view(const gmes_batch& b) {
   return v;
 }
 
+// Host copies of the descriptors of the last kHostBatches prepared batches,
+// keyed by workspace address: gmes_batch_step passes them to the multi-grid
+// cell kernel as launch arguments (batches of at most kParamJobs grids).
+// A workspace prepared again replaces its entry.
+constexpr int kHostBatches = 64;
+struct HostBatch {
+  const void* workspace = nullptr;
+  std::vector<GridDev> jobs;
+};
+std::mutex g_host_batch_mutex;
+HostBatch g_host_batches[kHostBatches];
+int g_host_batch_next = 0;
+
+void remember_batch(const void* ws, const GridDev* jobs, int njobs) {
+  std::lock_guard<std::mutex> lock(g_host_batch_mutex);
+  HostBatch* slot = nullptr;
+  for (auto& h : g_host_batches)
+    if (h.workspace == ws) slot = &h;
+  if (slot == nullptr) slot = &g_host_batches[g_host_batch_next++ % kHostBatches];
+  slot->workspace = ws;
+  slot->jobs.assign(jobs, jobs + njobs);
+}
+
+// The remembered descriptors of the batch in `ws` (empty if unknown or of
+// another size).
+std::vector<GridDev> recall_batch(const void* ws, int njobs) {
+  std::lock_guard<std::mutex> lock(g_host_batch_mutex);
+  for (const auto& h : g_host_batches)
+    if (h.workspace == ws && (int)h.jobs.size() == njobs) return h.jobs;
+  return {};
+}
+
 int64_t max_ghost_plane(const GridDev& d) {
   int64_t m = 1;
   for (int c = 0; c < 6; ++c)
@@ -581,6 +613,7 @@ gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs
   out->ghosts = gp[njobs];
   out->workspace = workspace;
   out->workspace_bytes = workspace_bytes;
+  remember_batch(workspace, jobs, njobs);
   return GMES_OK;
 }
 
@@ -602,7 +635,10 @@ gmes_status gmes_batch_step(const gmes_batch* b, int32_t nsteps, int32_t blocks,
   if (nsteps < 0 || blocks < 0) return fail(GMES_ERR_VALUE, "negative nsteps or blocks");
   if (b->njobs < 1) return fail(GMES_ERR_VALUE, "empty batch");
   if (nsteps == 0) return GMES_OK;
-  cudaError_t e = launch_batch(batch_view(*b), b->precision, b->dispersive != 0, nsteps, blocks,
+  const std::vector<GridDev> host =
+      b->njobs <= kParamJobs ? recall_batch(b->workspace, b->njobs) : std::vector<GridDev>();
+  cudaError_t e = launch_batch(batch_view(*b), host.empty() ? nullptr : host.data(),
+                               b->precision, b->dispersive != 0, nsteps, blocks,
                                static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "launching batch kernels");
   return GMES_OK;
@@ -1177,7 +1213,7 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
   b.workspace = g_noalloc_addr[dev];
   b.workspace_bytes = kNoAllocBytes;
   if (nsteps == 0) return GMES_OK;
-  e = launch_batch(batch_view(b), precision, disp, nsteps, 0, s);
+  e = launch_batch(batch_view(b), jobs, precision, disp, nsteps, 0, s);
   if (e != cudaSuccess) return cuda_fail(e, "launching batch kernels");
   return GMES_OK;
 }

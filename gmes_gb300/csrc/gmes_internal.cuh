@@ -408,8 +408,20 @@ GridDev make_grid_dev(const gmes_grid_desc& g);
 cudaError_t launch_step(const gmes_grid_desc& g, const Plan& p, int nsteps, cudaStream_t s);
 cudaError_t launch_half(const gmes_grid_desc& g, const Plan& p, int side, int step,
                         cudaStream_t s);
-cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nsteps, int blocks,
-                         cudaStream_t s);
+// The descriptors of a batch of at most kParamJobs grids, passed by value
+// to the multi-grid cell kernel (kernel arguments are limited to 32764
+// bytes), so that a cell reads its grid's fields from the argument bank as
+// the single-grid kernel does.
+constexpr int kParamJobs = 20;
+struct BatchDescs {
+  GridDev jobs[kParamJobs];
+};
+static_assert(sizeof(BatchDescs) + 512 <= 32764, "batch descriptors exceed the argument space");
+
+// host_jobs: host copies of the batch's descriptors (v.jobs), or NULL; with
+// them a batch of at most kParamJobs grids may take the argument-bank kernel.
+cudaError_t launch_batch(const BatchView& v, const GridDev* host_jobs, int precision, bool disp,
+                         int nsteps, int blocks, cudaStream_t s);
 cudaError_t launch_raster(const gmes_grid_desc& gd, const GridDev& d, int c,
                           const gmes_shape* shapes, int nshapes, const uint8_t* lut,
                           cudaStream_t s);

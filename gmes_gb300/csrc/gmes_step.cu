@@ -20,6 +20,8 @@
 //              D1 = E_{a2}[x + e_a1] - E_{a2}[x],  D2 = E_{a1}[x + e_a2] - E_{a1}[x]
 // which is exactly the (in1, in2, d1, d2) binding of gmes/fdtd.py:673-809
 // and the stencils of src/pw_dielectric.hh:118-371.
+#include <cstring>
+
 #include "gmes_internal.cuh"
 
 namespace gmes {
@@ -37,7 +39,8 @@ namespace {
 // (256^3 cube, Gcell/s):
 //   FP64  7 blocks (72 registers) 17.29   8 (64) 18.48   9 (56) 18.90
 //   FP32  10 blocks (48) 34.31           11 (46) 39.40  12 (40) 39.42
-//   df64  7 blocks 20.44                 8 (64) 22.33   9 (56) 22.60
+//   df64  7 blocks 20.44                 8 (64) 22.33   9 (56) 22.60  10 (48) 24.19
+//   (FP64 at 10 blocks 18.71; FP32 at 14 or 16 blocks, spilling, 35.7)
 // FP32 is bound by the loads in flight, so extra resident warps pay most
 // there; FP64 is bound by its pipe.  GMES_CELL_BLOCKS_F64 / _F32 / _DF
 // override them (tuning builds).
@@ -48,7 +51,7 @@ namespace {
 #define GMES_CELL_BLOCKS_F32 12
 #endif
 #ifndef GMES_CELL_BLOCKS_DF
-#define GMES_CELL_BLOCKS_DF 9
+#define GMES_CELL_BLOCKS_DF 10
 #endif
 template <class P>
 struct CellMinBlocks {
@@ -61,6 +64,59 @@ struct CellMinBlocks<PolF32> {
 template <>
 struct CellMinBlocks<PolDF> {
   static constexpr int value = GMES_CELL_BLOCKS_DF * 128 / kCellThreads;
+};
+// The multi-grid cell kernels carry a tile loop and a grid look-up on top of
+// the cell body (GMES_MULTI_BLOCKS_F64 / _F32 / _DF override the budgets).
+// Measured on GB300 (one 160^3 cube in a batch, descriptors as launch
+// arguments, ms per step): FP32 at 8 / 10 / 12 blocks 0.203 / 0.174 / 0.187;
+// FP64 at 7 / 8 / 9 blocks 0.304 / 0.302 / 0.292.
+#ifndef GMES_MULTI_BLOCKS_F64
+#define GMES_MULTI_BLOCKS_F64 9
+#endif
+#ifndef GMES_MULTI_BLOCKS_F32
+#define GMES_MULTI_BLOCKS_F32 10
+#endif
+#ifndef GMES_MULTI_BLOCKS_DF
+#define GMES_MULTI_BLOCKS_DF 10
+#endif
+template <class P>
+struct MultiMinBlocks {
+  static constexpr int value = GMES_MULTI_BLOCKS_F64 * 128 / kBatchThreads;
+};
+template <>
+struct MultiMinBlocks<PolF32> {
+  static constexpr int value = GMES_MULTI_BLOCKS_F32 * 128 / kBatchThreads;
+};
+template <>
+struct MultiMinBlocks<PolDF> {
+  static constexpr int value = GMES_MULTI_BLOCKS_DF * 128 / kBatchThreads;
+};
+// Whether a batch of at most kParamJobs grids takes its descriptors from
+// the argument bank (k_multi_cell_arg) or copies them to shared memory per
+// block (k_multi_cell); GMES_MULTI_ARG_F64 / _F32 / _DF override it.
+// Measured on GB300 (one 160^3 cube in a batch, ms per step, argument bank
+// / shared memory, single-grid kernel): FP32 0.173 / 0.194 (0.148), df64
+// 0.266 / 0.290 (0.220), FP64 0.289 / 0.279 (0.265).
+#ifndef GMES_MULTI_ARG_F64
+#define GMES_MULTI_ARG_F64 0
+#endif
+#ifndef GMES_MULTI_ARG_F32
+#define GMES_MULTI_ARG_F32 1
+#endif
+#ifndef GMES_MULTI_ARG_DF
+#define GMES_MULTI_ARG_DF 1
+#endif
+template <class P>
+struct ArgDescs {
+  static constexpr bool value = GMES_MULTI_ARG_F64 != 0;
+};
+template <>
+struct ArgDescs<PolF32> {
+  static constexpr bool value = GMES_MULTI_ARG_F32 != 0;
+};
+template <>
+struct ArgDescs<PolDF> {
+  static constexpr bool value = GMES_MULTI_ARG_DF != 0;
 };
 
 template <int C>
@@ -1049,7 +1105,7 @@ static_assert(sizeof(GridDev) % 16 == 0, "GridDev is copied as 16-byte words");
 // the single-grid kernel, whose descriptor is a kernel parameter; from
 // shared memory it runs 1.3x slower (measured on GB300, 160^3 cube).
 template <class P, int SIDE, bool STRICT, bool DISP>
-__global__ void __launch_bounds__(kBatchThreads, CellMinBlocks<P>::value)
+__global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P>::value)
     k_multi_cell(const BatchView v, int s) {
   __shared__ __align__(16) unsigned char desc[sizeof(GridDev)];
   const GridDev& g = *reinterpret_cast<const GridDev*>(desc);
@@ -1075,14 +1131,47 @@ __global__ void __launch_bounds__(kBatchThreads, CellMinBlocks<P>::value)
     const int bxl = __ldg(v.bxl + job);
     const int bx = 1 << bxl, by = kBatchThreads >> bxl;
     const int nkb = (g.n[2] + bx - 1) / bx, njb = (g.n[1] + by - 1) / by;
-    const int64_t local = b - __ldg(v.tile_prefix + job);
-    const int i = (int)(local / ((int64_t)nkb * njb));
-    const int rem = (int)(local - (int64_t)i * nkb * njb);
-    const int jb = rem / nkb, kb = rem - jb * nkb;
+    // a grid has fewer than 2^31 tiles: 32-bit unsigned divisions
+    const unsigned local = (unsigned)(b - __ldg(v.tile_prefix + job));
+    const unsigned plane = (unsigned)nkb * (unsigned)njb;
+    const int i = (int)(local / plane);
+    const unsigned rem = local - (unsigned)i * plane;
+    const int jb = (int)(rem / (unsigned)nkb), kb = (int)(rem - (unsigned)jb * nkb);
     const int k = kb * bx + (threadIdx.x & (bx - 1));
     const int j = jb * by + (threadIdx.x >> bxl);
     // batched grids hold fewer than 2^31 points per component (checked when
     // the batch is prepared)
+    if (k < g.n[2] && j < g.n[1]) {
+      if constexpr (STRICT)
+        cell_body<P, SIDE, STRICT, DISP, 0, int32_t>(g, i, j, k);
+      else
+        cell_body_fast<P, SIDE, DISP, 0, int32_t>(g, i, j, k);
+    }
+  }
+}
+
+// The same with the descriptors in the kernel's argument bank (batches of
+// at most kParamJobs grids): no shared-memory copy and no barrier per tile.
+template <class P, int SIDE, bool STRICT, bool DISP>
+__global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P>::value)
+    k_multi_cell_arg(const BatchView v, int s, const __grid_constant__ BatchDescs d) {
+  const int64_t per = (v.tiles + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = (int64_t)blockIdx.x * per;
+  const int64_t b1 = b0 + per < v.tiles ? b0 + per : v.tiles;
+  for (int64_t b = b0; b < b1; ++b) {
+    const int job = find_job<int64_t>(v.tile_prefix, v.njobs, b);  // block-uniform
+    if (s >= __ldg(v.steps + job)) continue;
+    const GridDev& g = d.jobs[job];
+    const int bxl = __ldg(v.bxl + job);
+    const int bx = 1 << bxl, by = kBatchThreads >> bxl;
+    const int nkb = (g.n[2] + bx - 1) / bx, njb = (g.n[1] + by - 1) / by;
+    const unsigned local = (unsigned)(b - __ldg(v.tile_prefix + job));
+    const unsigned plane = (unsigned)nkb * (unsigned)njb;
+    const int i = (int)(local / plane);
+    const unsigned rem = local - (unsigned)i * plane;
+    const int jb = (int)(rem / (unsigned)nkb), kb = (int)(rem - (unsigned)jb * nkb);
+    const int k = kb * bx + (threadIdx.x & (bx - 1));
+    const int j = jb * by + (threadIdx.x >> bxl);
     if (k < g.n[2] && j < g.n[1]) {
       if constexpr (STRICT)
         cell_body<P, SIDE, STRICT, DISP, 0, int32_t>(g, i, j, k);
@@ -1197,16 +1286,32 @@ cudaError_t dispatch_precision(const gmes_grid_desc& g, const Plan& p, int nstep
 }  // namespace
 
 template <class P, bool STRICT>
-cudaError_t run_batch(const BatchView& v, bool disp, int nsteps, int blocks, cudaStream_t st) {
+cudaError_t run_batch(const BatchView& v, const GridDev* host_jobs, bool disp, int nsteps,
+                      int blocks, cudaStream_t st) {
   using T = typename P::T;
   const int cells = blocks > 0 ? blocks : (int)(v.tiles < (1 << 30) ? v.tiles : (1 << 30));
   const int gblocks = (int)((v.ghosts + 255) / 256 < 65535 * 16 ? (v.ghosts + 255) / 256 : 65535 * 16);
   const int sblocks = (v.srcs + 127) / 128;
+  const bool arg = ArgDescs<P>::value && host_jobs != nullptr && v.njobs <= kParamJobs;
+  static thread_local BatchDescs descs;
+  if (arg) {
+    std::memset(&descs, 0, sizeof(descs));
+    for (int q = 0; q < v.njobs; ++q) descs.jobs[q] = host_jobs[q];
+  }
   for (int s = 0; s < nsteps; ++s) {
     for (int side = 0; side < 2; ++side) {
       if (gblocks > 0) k_multi_ghost<T><<<gblocks, 256, 0, st>>>(v, 1 - side, s);
       if (cells > 0) {
-        if (side == 0) {
+        if (arg) {
+          if (side == 0) {
+            if (disp)
+              k_multi_cell_arg<P, 0, STRICT, true><<<cells, kBatchThreads, 0, st>>>(v, s, descs);
+            else
+              k_multi_cell_arg<P, 0, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s, descs);
+          } else {
+            k_multi_cell_arg<P, 1, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s, descs);
+          }
+        } else if (side == 0) {
           if (disp)
             k_multi_cell<P, 0, STRICT, true><<<cells, kBatchThreads, 0, st>>>(v, s);
           else
@@ -1221,17 +1326,17 @@ cudaError_t run_batch(const BatchView& v, bool disp, int nsteps, int blocks, cud
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const BatchView& v, int precision, bool disp, int nsteps, int blocks,
-                         cudaStream_t s) {
+cudaError_t launch_batch(const BatchView& v, const GridDev* host_jobs, int precision, bool disp,
+                         int nsteps, int blocks, cudaStream_t s) {
   switch (precision) {
     case GMES_FP64:
-      return run_batch<PolF64, false>(v, disp, nsteps, blocks, s);
+      return run_batch<PolF64, false>(v, host_jobs, disp, nsteps, blocks, s);
     case GMES_FP64_STRICT:
-      return run_batch<PolF64, true>(v, disp, nsteps, blocks, s);
+      return run_batch<PolF64, true>(v, host_jobs, disp, nsteps, blocks, s);
     case GMES_FP32:
-      return run_batch<PolF32, false>(v, disp, nsteps, blocks, s);
+      return run_batch<PolF32, false>(v, host_jobs, disp, nsteps, blocks, s);
     case GMES_DF64:
-      return run_batch<PolDF, false>(v, disp, nsteps, blocks, s);
+      return run_batch<PolDF, false>(v, host_jobs, disp, nsteps, blocks, s);
     default:
       return cudaErrorInvalidValue;
   }

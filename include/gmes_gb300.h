@@ -354,6 +354,10 @@ gmes_status gmes_batch_set_steps(const gmes_batch* b, const int32_t* steps, void
  * per tile).
  */
 gmes_status gmes_batch_step(const gmes_batch* b, int32_t nsteps, int32_t blocks, void* stream);
+/* (For batches of at most 20 grids the cell kernel takes the grids'
+   descriptors as launch arguments: gmes_batch_prepare keeps a host copy of
+   the last 64 prepared batches' descriptors, keyed by workspace address.
+   Results are the same either way.) */
 
 /*
  * Batch step that allocates nothing.  No counterpart in the reference.

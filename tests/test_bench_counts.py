@@ -11,15 +11,13 @@ def _prob(nsteps, segment, keep):
 
 
 def _adj_chunks(k, per):
-    # the library's adjoint chunks: odd counts of at most ``per`` steps
-    n = 0
-    while k > 0:
-        m = min(k, per)
-        if m % 2 == 0:
-            m -= 1
-        k -= m
+    # the library's adjoint launches: the fewest of at most ``per`` steps
+    # whose count has the parity of k (the psi-adjoint buffers alternate per
+    # launch and must end where the step-parity convention puts them)
+    n = -(-k // per)
+    while n % 2 != k % 2:
         n += 1
-    return n
+    return min(n, k)
 
 
 @pytest.mark.parametrize("nsteps,segment", [(2000, 45), (160, 7), (37, 37), (1, 1)])
@@ -40,5 +38,6 @@ def test_design_launch_count(nsteps, segment):
 
 
 def test_adjoint_chunks_of_the_default_workload():
-    # 2000 steps: 666 launches of 3 steps, then two of 1
-    assert _adj_chunks(2000, 4) == 668
+    # 2000 steps: 500 launches of 4; a 45-step segment: 13 launches (odd)
+    assert _adj_chunks(2000, 4) == 500
+    assert _adj_chunks(45, 4) == 13 and _adj_chunks(2, 4) == 2 and _adj_chunks(1, 4) == 1

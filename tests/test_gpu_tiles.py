@@ -41,6 +41,7 @@ CASES_RUN = [("cube45", "fp64"), ("cube45", "fp32"), ("cube45", "df64"),
              ("disp40", "df64"), ("drude2d", "fp64"), ("air2d", "fp64"), ("air2d", "fp32"),
              ("bloch48", "fp64")]
 
+
 def _bloch48(precision):
     """Complex fields with a Bloch vector (as the bloch3d golden scene) on a
     48^3 grid, so that whole 16-cell rows lie inside the PML-free interior."""
