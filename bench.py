@@ -196,6 +196,30 @@ def ncu_pipe(workload_key, precision, side="E"):
     return _profile_entry("pipes.json", workload_key, precision, side)
 
 
+def fp64_pipe_ceiling(workload_key, precision, value, clocks):
+    """The FP64 pipe's bound on the step rate, beside the HBM roofline.
+
+    GB300 issues one FP64 warp-instruction per 16 SM cycles (1.0 TFLOP/s
+    FP64 FMA measured: 2 lanes per clock per SM), so with n FP64
+    instructions per cell and half-step (committed ncu count, both halves)
+    the step rate cannot pass SMs x clock / 16 x 32 / (2 n) cells per second.
+    """
+    if precision not in ("fp64",):
+        return None
+    e = ncu_pipe(workload_key, precision, "E")
+    if not e or "fp64_inst_per_cell" not in e:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    per_step = 2 * float(e["fp64_inst_per_cell"])
+    ceiling = sms * mhz * 1e6 / 16 * 32 / per_step / 1e9
+    return {"ceiling_gcells": round(ceiling, 3), "fraction_of_ceiling": round(value / ceiling, 4),
+            "fp64_inst_per_cell_step": per_step, "sms": sms, "sm_mhz": mhz,
+            "note": "the FP64 step is bound by the FP64 pipe, not HBM; roofline.frac stays "
+                    "the HBM fraction"}
+
+
 # ---------------------------------------------------------------------------
 # algorithmic bytes
 # ---------------------------------------------------------------------------
@@ -392,6 +416,7 @@ def run_ours(args):
                      "launch_ms": round(dom[2], 5), "peak_source": peak_src,
                      "pipe": ncu_pipe(cfg["workload"], args.precision, side)},
         "half_ms": {"E": round(e_ms, 5), "H": round(h_ms, 5)},
+        "fp64_pipe": fp64_pipe_ceiling(cfg["workload"], args.precision, value, clocks),
         "gpu_launches": args.steps * (6 if scene.sources else 4),
         "clocks": clocks,
     }

@@ -22,6 +22,8 @@
 // and the stencils of src/pw_dielectric.hh:118-371.
 #include <cstring>
 
+#include <type_traits>
+
 #include "gmes_internal.cuh"
 
 namespace gmes {
@@ -223,6 +225,76 @@ __device__ __forceinline__ R plain_upd(R F, R c1, R c2, R p1, R p2) {
   return E ? plain_e(F, c1, c2, p1, p2) : plain_e(F, c2, c1, p2, p1);
 }
 
+// a b + c, fused explicitly (float-float: its own exact operations), so that
+// the CPML update rounds the same wherever it is inlined.
+__device__ __forceinline__ double madd(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float madd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ df madd(df a, df b, df c) { return a * b + c; }
+
+// Update of a CPML point in the separate form (src/pw_cpml.hh:115-132 E,
+// 327-344 H): psi1 = b1 psi1 + (c1/d1) D1 and psi2 likewise where the point
+// is inside that axis' slab (c != 0; elsewhere psi stays exactly 0), then
+// F +/- cdt ((psi1 - psi2) + D1/(kappa1 d1) - D2/(kappa2 d2)); a point
+// outside both slabs takes the dielectric form.  Per point in update_fast,
+// and for warps of one class per component in cell_body_fast.
+template <class P, int C>
+__device__ __forceinline__ void cpml_separate(const GridDev& g, int64_t lin, const int x[3],
+                                              typename P::R p1, typename P::R p2,
+                                              typename P::R F, const ClassCoef& cc,
+                                              Pre<P> pre) {
+  using R = typename P::R;
+  using T = typename P::T;
+  constexpr int own = C % 3, a1 = (own + 1) % 3, a2 = (own + 2) % 3;
+  constexpr bool E = C < 3;
+  T* fp = static_cast<T*>(g.f[C]) + lin;
+  T* aux = static_cast<T*>(g.aux[C]);
+  const int64_t np = g.npts[C];
+  const int pm = __ldg(&cc.pml);
+  const Coef* q1 = g.prof[pm][C][a1] + (int64_t)x[a1] * kProfStride;
+  const Coef* q2 = g.prof[pm][C][a2] + (int64_t)x[a2] * kProfStride;
+  const bool on1 = coef_nonzero(q1 + 1), on2 = coef_nonzero(q2 + 1);
+  if (!on1 && !on2) {
+    // outside both slabs kappa = 1 and psi = 0: the dielectric update
+    const R c1 = P::cfg(&cc.c1), c2 = P::cfg(&cc.c2);
+    P::st(fp, plain_upd<E>(F, c1, c2, p1, p2));
+    return;
+  }
+  R psi1 = pre.a, psi2 = pre.b;
+  if constexpr (PsiVote<P>::value) {
+    // A warp-wide vote before each psi update: the compiler otherwise
+    // predicates the short update blocks, and every warp of the shell then
+    // issues their instructions whether or not a lane is in that slab.
+    // Each lane still keeps its own value (psi changes only where on).
+    const unsigned am = __activemask();
+    if (__any_sync(am, on1)) {
+      const R n1 = madd(P::cfg(q1 + 3), p1, P::cfg(q1) * psi1);
+      if (on1) {
+        psi1 = n1;
+        P::st(aux + lin, psi1);
+      }
+    }
+    if (__any_sync(am, on2)) {
+      const R n2 = madd(P::cfg(q2 + 3), p2, P::cfg(q2) * psi2);
+      if (on2) {
+        psi2 = n2;
+        P::st(aux + np + lin, psi2);
+      }
+    }
+  } else {
+    if (on1) {
+      psi1 = madd(P::cfg(q1 + 3), p1, P::cfg(q1) * psi1);
+      P::st(aux + lin, psi1);
+    }
+    if (on2) {
+      psi2 = madd(P::cfg(q2 + 3), p2, P::cfg(q2) * psi2);
+      P::st(aux + np + lin, psi2);
+    }
+  }
+  const R X = madd(-P::cfg(q2 + 4), p2, madd(P::cfg(q1 + 4), p1, psi1 - psi2));
+  const R cdt = P::cfg(&cc.cdt);
+  P::st(fp, E ? madd(cdt, X, F) : madd(-cdt, X, F));
+}
+
 template <class P, int C, bool DISP>
 __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const int x[3],
                                             typename P::R p1, typename P::R p2,
@@ -289,39 +361,20 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
   T* aux = static_cast<T*>(g.aux[C]);
   const int64_t np = g.npts[C];
   if (kind == GMES_KIND_CPML) {
-    // Where a profile's c coefficient is (+/-)0 -- outside that axis' slab --
-    // psi stays exactly 0 (b * 0 + 0 * D), so its update is skipped.
-    const Coef* q1 = g.prof[__ldg(&cc.pml)][C][a1] + (int64_t)x[a1] * kProfStride;
-    const Coef* q2 = g.prof[__ldg(&cc.pml)][C][a2] + (int64_t)x[a2] * kProfStride;
-    const bool on1 = coef_nonzero(q1 + 1), on2 = coef_nonzero(q2 + 1);
-    if (!on1 && !on2) {
-      // outside both slabs kappa = 1 and psi = 0: the dielectric update
-      const R c1 = P::cfg(&cc.c1), c2 = P::cfg(&cc.c2);
-      P::st(fp, plain_upd<E>(F, c1, c2, p1, p2));
-      return;
-    }
-    R psi1 = pre.a, psi2 = pre.b;
-    if constexpr (PsiVote<P>::value) {
-      // A warp-wide vote before each psi update: the compiler otherwise
-      // predicates the short update blocks, and every warp of the shell then
-      // issues their FP64 instructions whether or not a lane is in that slab.
-      // Each lane still keeps its own value (psi changes only where on).
-      const unsigned am = __activemask();
-      if (__any_sync(am, on1)) {
-        const R n1 = P::cfg(q1) * psi1 + P::cfg(q1 + 3) * p1;
-        if (on1) {
-          psi1 = n1;
-          P::st(aux + lin, psi1);
-        }
-      }
-      if (__any_sync(am, on2)) {
-        const R n2 = P::cfg(q2) * psi2 + P::cfg(q2 + 3) * p2;
-        if (on2) {
-          psi2 = n2;
-          P::st(aux + np + lin, psi2);
-        }
-      }
+    if constexpr (!std::is_same<P, PolDF>::value) {
+      cpml_separate<P, C>(g, lin, x, p1, p2, F, cc, pre);
     } else {
+      // the float-float type keeps this block inline: in cpml_separate it
+      // spilled more and ran 1.5 % slower (256^3 cube, 24.21 -> 23.84
+      // Gcell/s); the arithmetic is the same, term for term
+      const Coef* q1 = g.prof[__ldg(&cc.pml)][C][a1] + (int64_t)x[a1] * kProfStride;
+      const Coef* q2 = g.prof[__ldg(&cc.pml)][C][a2] + (int64_t)x[a2] * kProfStride;
+      const bool on1 = coef_nonzero(q1 + 1), on2 = coef_nonzero(q2 + 1);
+      if (!on1 && !on2) {
+        P::st(fp, plain_upd<E>(F, P::cfg(&cc.c1), P::cfg(&cc.c2), p1, p2));
+        return;
+      }
+      R psi1 = pre.a, psi2 = pre.b;
       if (on1) {
         psi1 = P::cfg(q1) * psi1 + P::cfg(q1 + 3) * p1;
         P::st(aux + lin, psi1);
@@ -330,10 +383,10 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
         psi2 = P::cfg(q2) * psi2 + P::cfg(q2 + 3) * p2;
         P::st(aux + np + lin, psi2);
       }
+      const R X = ((psi1 - psi2) + P::cfg(q1 + 4) * p1) - P::cfg(q2 + 4) * p2;
+      const R cdt = P::cfg(&cc.cdt);
+      P::st(fp, E ? F + cdt * X : F - cdt * X);
     }
-    const R X = ((psi1 - psi2) + P::cfg(q1 + 4) * p1) - P::cfg(q2 + 4) * p2;
-    const R cdt = P::cfg(&cc.cdt);
-    P::st(fp, E ? F + cdt * X : F - cdt * X);
     return;
   }
   const R r1 = P::cf(g.rdr[a1]);
@@ -733,6 +786,39 @@ __device__ __forceinline__ void cell_body(const GridDev& g, int i, int j, int k)
   }
 }
 
+// Whether a warp whose class triple is uniform, with DIELECTRIC or CPML
+// classes (the CPML shell), takes those kinds' updates directly instead of
+// the per-point kind dispatch.  Measured on GB300 (256^3 cube, Gcell/s, one
+// box): FP32 39.78 -> 40.64; with it df64 ran 24.21 -> 23.01 and FP64 18.90
+// -> 18.91, so only FP32 takes it (GMES_UNIFORM_CPML = 1 gives it every
+// precision, 0 none).  The CPML update it shares with the per-point path
+// (cpml_separate) fuses every multiply-add explicitly: inlined in two places
+// with implicit contraction, the two copies rounded differently and a grid
+// batched with another warp layout lost bit-identity with its solo run.
+template <class P>
+struct UniformCpml {
+#if defined(GMES_UNIFORM_CPML)
+  static constexpr bool value = GMES_UNIFORM_CPML != 0;
+#else
+  static constexpr bool value = false;
+#endif
+};
+template <>
+struct UniformCpml<PolF32> {
+#if defined(GMES_UNIFORM_CPML)
+  static constexpr bool value = GMES_UNIFORM_CPML != 0;
+#else
+  static constexpr bool value = true;
+#endif
+};
+
+// The psi pair (psi1, psi2) of a CPML point of component c.
+template <class P>
+__device__ __forceinline__ Pre<P> psi_pair(const GridDev& g, int c, int64_t lin) {
+  const typename P::T* aux = static_cast<const typename P::T*>(g.aux[c]);
+  return {P::ldw(aux + lin), P::ldw(aux + g.npts[c] + lin)};
+}
+
 // The half-step update of one cell in the fast precisions.  Every field
 // value and class id the cell reads is loaded first, so that no load waits
 // for another.  Then a warp whose cells all carry the same class triple, each
@@ -800,11 +886,25 @@ __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, i
   const uint32_t t = (uint32_t)id0 | (uint32_t)id1 << 8 | (uint32_t)id2 << 16;
   int same = 0;
   __match_all_sync(__activemask(), t, &same);
-  const bool fast =
-      same && !g.pointwise &&
-      (!is_active<MASK, c0>(g) || g.tab[c0][id0].kind == GMES_KIND_DIELECTRIC) &&
-      (!is_active<MASK, c0 + 1>(g) || g.tab[c0 + 1][id1].kind == GMES_KIND_DIELECTRIC) &&
-      (!is_active<MASK, c0 + 2>(g) || g.tab[c0 + 2][id2].kind == GMES_KIND_DIELECTRIC);
+  const bool uniform = same && !g.pointwise;
+  // the warp's kinds when its class triple is uniform (inactive components
+  // count as dielectric: they are skipped)
+  int ka = GMES_KIND_DIELECTRIC, kb = GMES_KIND_DIELECTRIC, kc = GMES_KIND_DIELECTRIC;
+  bool fast;
+  if constexpr (UniformCpml<P>::value) {
+    if (uniform) {
+      if (is_active<MASK, c0>(g)) ka = g.tab[c0][id0].kind;
+      if (is_active<MASK, c0 + 1>(g)) kb = g.tab[c0 + 1][id1].kind;
+      if (is_active<MASK, c0 + 2>(g)) kc = g.tab[c0 + 2][id2].kind;
+    }
+    fast = uniform && ka == GMES_KIND_DIELECTRIC && kb == GMES_KIND_DIELECTRIC &&
+           kc == GMES_KIND_DIELECTRIC;
+  } else {
+    fast = uniform &&
+           (!is_active<MASK, c0>(g) || g.tab[c0][id0].kind == GMES_KIND_DIELECTRIC) &&
+           (!is_active<MASK, c0 + 1>(g) || g.tab[c0 + 1][id1].kind == GMES_KIND_DIELECTRIC) &&
+           (!is_active<MASK, c0 + 2>(g) || g.tab[c0 + 2][id2].kind == GMES_KIND_DIELECTRIC);
+  }
   constexpr bool E = SIDE == 0;
   if (fast) {  // warp-uniform
     const ClassCoef& qa = g.tab[c0][id0];
@@ -820,6 +920,42 @@ __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, i
       P::st(static_cast<T*>(g.f[c0 + 2]) + l2,
             plain_upd<E>(f2, P::cfg(&qc.c1), P::cfg(&qc.c2), d21, d22));
     return;
+  }
+  if constexpr (UniformCpml<P>::value) {
+    const auto dc = [](int kd) {
+      return kd == GMES_KIND_DIELECTRIC || kd == GMES_KIND_CPML;
+    };
+    if (uniform && dc(ka) && dc(kb) && dc(kc)) {
+      // one class per component across the warp, each DIELECTRIC or CPML
+      // (the CPML shell): those kinds' updates with the kinds known for the
+      // whole warp, the psi values of the CPML components loaded first
+      const int xa[3] = {i, SIDE == 0 ? j : j + 1, SIDE == 0 ? k : k + 1};
+      const int xb[3] = {SIDE == 0 ? i : i + 1, j, SIDE == 0 ? k : k + 1};
+      const int xq[3] = {SIDE == 0 ? i : i + 1, SIDE == 0 ? j : j + 1, k};
+      Pre<P> pa{P::zero(), P::zero()}, pb = pa, pc = pa;
+      if (ka == GMES_KIND_CPML) pa = psi_pair<P>(g, c0, l0);
+      if (kb == GMES_KIND_CPML) pb = psi_pair<P>(g, c0 + 1, l1);
+      if (kc == GMES_KIND_CPML) pc = psi_pair<P>(g, c0 + 2, l2);
+      const ClassCoef& qa = g.tab[c0][id0];
+      const ClassCoef& qb = g.tab[c0 + 1][id1];
+      const ClassCoef& qc = g.tab[c0 + 2][id2];
+      if (ka == GMES_KIND_CPML)
+        cpml_separate<P, c0>(g, l0, xa, d01, d02, f0, qa, pa);
+      else if (is_active<MASK, c0>(g))
+        P::st(static_cast<T*>(g.f[c0]) + l0,
+              plain_upd<E>(f0, P::cfg(&qa.c1), P::cfg(&qa.c2), d01, d02));
+      if (kb == GMES_KIND_CPML)
+        cpml_separate<P, c0 + 1>(g, l1, xb, d11, d12, f1, qb, pb);
+      else if (is_active<MASK, c0 + 1>(g))
+        P::st(static_cast<T*>(g.f[c0 + 1]) + l1,
+              plain_upd<E>(f1, P::cfg(&qb.c1), P::cfg(&qb.c2), d11, d12));
+      if (kc == GMES_KIND_CPML)
+        cpml_separate<P, c0 + 2>(g, l2, xq, d21, d22, f2, qc, pc);
+      else if (is_active<MASK, c0 + 2>(g))
+        P::st(static_cast<T*>(g.f[c0 + 2]) + l2,
+              plain_upd<E>(f2, P::cfg(&qc.c1), P::cfg(&qc.c2), d21, d22));
+      return;
+    }
   }
   if constexpr (SIDE == 0) {
     const int xc[3] = {i, j, k};
