@@ -92,7 +92,10 @@ __host__ __device__ inline int64_t align256(int64_t x) { return (x + 255) & ~int
 #endif
 constexpr int kCellThreads = GMES_CELL_THREADS;
 constexpr int kCellWarps = kCellThreads / 32;
-constexpr int kRowLog2 = 4;
+#ifndef GMES_ROW_LOG2
+#define GMES_ROW_LOG2 4
+#endif
+constexpr int kRowLog2 = GMES_ROW_LOG2;
 
 struct CellTiling {
   int bx_log2, bx, by, nkb, njb;

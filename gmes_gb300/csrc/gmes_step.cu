@@ -163,13 +163,11 @@ __device__ __forceinline__ Pre<P> prefetch_state(const GridDev& g, int64_t lin, 
 // slower with it (19.6 -> 18.3; with a __syncwarp opening each voted block
 // and 16-cell rows, 21.05 -> 20.67).  Votes in front of the other kinds'
 // blocks were slower in every precision.
+// (The float-float type keeps plain branches in its own CPML block in
+// update_fast.)
 template <class P>
 struct PsiVote {
   static constexpr bool value = true;
-};
-template <>
-struct PsiVote<PolDF> {
-  static constexpr bool value = false;
 };
 
 // Whether a profile entry has kappa == 1 (the default CPML grading,
@@ -238,11 +236,10 @@ __device__ __forceinline__ R plain_upd(R F, R c1, R c2, R p1, R p2) {
   return E ? plain_e(F, c1, c2, p1, p2) : plain_e(F, c2, c1, p2, p1);
 }
 
-// a b + c, fused explicitly (float-float: its own exact operations), so that
-// the CPML update rounds the same wherever it is inlined.
+// a b + c, fused explicitly, so that the CPML update rounds the same wherever
+// it is inlined.
 __device__ __forceinline__ double madd(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float madd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-__device__ __forceinline__ df madd(df a, df b, df c) { return a * b + c; }
 
 // Update of a CPML point in the separate form (src/pw_cpml.hh:115-132 E,
 // 327-344 H): psi1 = b1 psi1 + (c1/d1) D1 and psi2 likewise where the point
