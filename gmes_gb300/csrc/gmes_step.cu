@@ -1074,6 +1074,40 @@ __global__ void k_ghost(const GridDev g, int side, int64_t maxplane) {
   ghost_point<T>(g, side, blockIdx.y, t);
 }
 
+// The same for grids whose components hold fewer than 2^31 points: 32-bit
+// index arithmetic (one unsigned division per point instead of a 64-bit
+// one).  Same points, same copies.
+template <class T>
+__global__ void k_ghost32(const GridDev g, int side, unsigned maxplane) {
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= maxplane) return;
+  const int item = blockIdx.y;
+  const int c = side * 3 + item / 2;
+  if (!(g.active & (1 << c))) return;
+  const int own = c % 3;
+  const int ga = (item & 1) ? (own + 2) % 3 : (own + 1) % 3;
+  const int pa = (ga + 1) % 3, qa = (ga + 2) % 3;
+  const int p_ = pa < qa ? pa : qa, q_ = pa < qa ? qa : pa;  // q_ is the faster axis
+  const unsigned sh[3] = {(unsigned)g.sh[c][0], (unsigned)g.sh[c][1], (unsigned)g.sh[c][2]};
+  if (t >= sh[p_] * sh[q_]) return;
+  unsigned x[3];
+  x[p_] = t / sh[q_];
+  x[q_] = t - x[p_] * sh[q_];
+  x[ga] = side == 0 ? sh[ga] - 1 : 0;
+  unsigned s[3] = {x[0], x[1], x[2]};
+  const int a1 = (own + 1) % 3, a2 = (own + 2) % 3;
+  if (side == 0) {
+    if (x[a1] == sh[a1] - 1) s[a1] = 0;
+    if (x[a2] == sh[a2] - 1) s[a2] = 0;
+  } else {
+    if (x[a1] == 0) s[a1] = sh[a1] - 1;
+    if (x[a2] == 0) s[a2] = sh[a2] - 1;
+  }
+  const unsigned st0 = (unsigned)g.st[c][0], st1 = (unsigned)g.st[c][1];
+  T* f = static_cast<T*>(g.f[c]);
+  f[x[0] * st0 + x[1] * st1 + x[2]] = f[s[0] * st0 + s[1] * st1 + s[2]];
+}
+
 // Ghost planes of a complex grid (Bloch boundary, gmes/fdtd.py:811-1097):
 // as ghost_point, but the value is multiplied by the phase factor of each
 // ghost axis in the reference's copy order (own+1, then own+2).  The
@@ -1373,6 +1407,8 @@ void run_half(const Plan& p, int side, int st, cudaStream_t s) {
   constexpr int kMaxY = 65535;
   if (p.cplx)
     k_ghost_c<STRICT><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
+  else if (offsets_fit_i32(d))
+    k_ghost32<T><<<ggrid, 256, 0, s>>>(d, 1 - side, (unsigned)maxplane);
   else
     k_ghost<T><<<ggrid, 256, 0, s>>>(d, 1 - side, maxplane);
   const CellTiling tl = cell_tiling(d.n);
