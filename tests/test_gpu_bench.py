@@ -21,7 +21,8 @@ def bench(*args):
 
 
 def test_cube_line():
-    d = bench("--n", "48", "--steps", "5", "--warmup", "3", "--no-cpu-baseline", "--no-variants")
+    d = bench("--n", "48", "--steps", "5", "--warmup", "3", "--no-cpu-baseline", "--no-variants",
+              "--no-serving")
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
                 "roofline", "e2e", "clocks", "gpu_launches"):
@@ -49,3 +50,17 @@ def test_design_line(segment, passes):
     assert d["value"] == pytest.approx(passes * cells * steps * 2 / per / 1e9, rel=1e-3)
     assert (d["config"]["checkpoints"] == 0) == (passes == 2)
     assert d["grad_finite"] and d["gpu_launches"] > 0
+
+
+def test_serving_line():
+    """A small serving run: batched against one at a time, latencies, and the
+    measured batching bound, consistent with each other."""
+    d = bench("--workload", "serving", "--jobs", "6", "--size-scale", "0.3",
+              "--max-job-steps", "300")
+    sv = d["serving"]
+    assert sv["failed"] == 0 and d["value"] == sv["batched_gcells"] > 0
+    assert sv["latency_p99_s"] >= sv["latency_p50_s"] > 0
+    assert sv["speedup"] == pytest.approx(sv["batched_gcells"] / sv["one_at_a_time_gcells"],
+                                          rel=2e-3)
+    assert sv["bound"] > 0
+    assert sv["speedup_over_bound"] == pytest.approx(sv["speedup"] / sv["bound"], rel=5e-3)
