@@ -844,7 +844,12 @@ __device__ __forceinline__ Pre<P> psi_pair(const GridDev& g, int c, int64_t lin)
 //   dispersive FP64 9.85 -> 10.09, FP32 20.48 -> 22.36, df64 14.85 -> 15.04.
 // A per-warp table of plain warps built at set-up (read with the field
 // values, class maps read only by the other warps) ran slower: cube FP64
-// 18.20, FP32 31.90, df64 22.95.
+// 18.20, FP32 31.90, df64 22.95.  So did two cells per thread, (i, j, k) and
+// (i + 1, j, k), with the loads of both issued before either update (twice
+// the bytes in flight per warp, four shared neighbour loads): cube FP32
+// 42.54 -> 30.1 / 29.7 / 34.3 / 31.1 Gcell/s at 6 / 7 / 8 / 10 blocks per SM
+// (64 registers at 8), dispersive FP32 25.42 -> 22.35; df64 (5, 6 blocks)
+// 26.74 -> 17.5 / 20.7, FP64 (6 blocks) 19.25 -> 16.99.
 template <class P, int SIDE, bool DISP, int MASK, class I>
 __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, int k) {
   using R = typename P::R;
