@@ -837,8 +837,10 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
   float* sLX = sLE + NP;
   float* sLY = sLX + NP;
   float* sP = sLY + NP;      // psi adjoints of Ez (x, y), Hx, Hy: sP + k * NP
-  float* sW1 = sP + 4 * NP;  // curl weights: Hx, then Ez's first
-  float* sW2 = sW1 + NP;     // curl weights: Hy, then Ez's second
+  float* sW1 = sP + 4 * NP;  // curl weights of the H half: Hx
+  float* sW2 = sW1 + NP;     //   and Hy
+  float* sV1 = sW2 + NP;     // curl weights of the E half: Ez's first
+  float* sV2 = sV1 + NP;     //   and its second
   const int c = threadIdx.x, ty = threadIdx.y, b = blockIdx.z;
   const int ri0 = (int)blockIdx.y * TI - H, rj0 = (int)blockIdx.x * TJ - H;
   const int j = wrap_index(rj0 + c, t.ny);
@@ -874,81 +876,100 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
   // as in k_tmz_tb_fwd: a copy of the loop without the CPML path for
   // regions that have no CPML point inside a profile
   const bool psi_any = __syncthreads_or(any & (kTmzPsiE | kTmzPsiX | kTmzPsiY)) != 0;
+  // Per step (n = n0 + s + 1, s from nsub - 1 down to 0), the transposes of
+  // the one-step kernels in their order: H-side sources, the curl weights
+  // of every Hx / Hy point (hw), lambda_E gathering them (eu), E-side
+  // sources, the curl weights of every Ez point and the gradient (ew),
+  // lambda_X / lambda_Y gathering those (xu).  A point's weights depend
+  // only on its own adjoints, so ew runs in the same pass as eu and the
+  // next step's hw in the same pass as xu (into other arrays than the
+  // neighbours read): two barriers per step.  A block holding a source
+  // point applies it between the two, with barriers around it.
   auto steps = [&](auto tag) {
     constexpr bool PSI = decltype(tag)::value;
+    auto hw = [&](int q) {
+      const int k = (ty + kTbRows * q) * RJ + c;
+      sW1[k] = (fl[q] & kTmzPlainX) ? pt[q].cxn * sLX[k]
+               : (PSI && (fl[q] & kTmzPsiX))
+                   ? adjx_cpml<P, true>(g, fl[q], pt[q].cxn, j, sLX[k], sP + 2 * NP + k,
+                                        sP + 2 * NP + k)
+                   : 0.f;
+      sW2[k] = (fl[q] & kTmzPlainY) ? pt[q].cy * sLY[k]
+               : (PSI && (fl[q] & kTmzPsiY))
+                   ? adjy_cpml<P, true>(g, fl[q], pt[q].cy, li[q], sLY[k], sP + 3 * NP + k,
+                                        sP + 3 * NP + k)
+                   : 0.f;
+    };
+    auto eu = [&](int q, int n) {
+      const int a = ty + kTbRows * q, k = a * RJ + c;
+      if (a >= 1 && c >= 1) {
+        float le = sLE[k];
+        if (fl[q] & kTmzMonitor) {
+          bool has;
+          le = le + P::from_double(seed_of(g, t, b, li[q], j, n, &has));
+        }
+        sLE[k] = le + ((sW1[k - 1] - sW1[k]) + (sW2[k - RJ] - sW2[k]));
+      }
+    };
+    auto ew = [&](int q, int n) {
+      const int k = (ty + kTbRows * q) * RJ + c;
+      float w1, w2;
+      if (fl[q] & kTmzPlainE) {
+        const float le = sLE[k];
+        w1 = pt[q].c1 * le;
+        w2 = pt[q].c2n * le;
+      } else {
+        w1 = w2 = 0.f;
+        if (PSI && (fl[q] & kTmzPsiE))
+          adje_cpml<P, true, true, true>(g, fl[q], pt[q].c1, li[q], j, sLE[k], sP + k, sP + k,
+                                         sP + NP + k, sP + NP + k, w1, w2);
+      }
+      sV1[k] = w1;
+      sV2[k] = w2;
+      if ((fl[q] & kTmzDesign) && (fl[q] >> 31)) {
+        const int64_t kk = (int64_t)b * nd + design_index(t, li[q], j);
+        const double le = (double)sLE[k];
+        const double inc = (double)static_cast<const float*>(
+            t.hist)[((int64_t)(n - step0 - 1) * t.nb + b) * nd + (kk - (int64_t)b * nd)];
+        t.grad[kk] += le * inc * t.dc[kk].neg_reps;
+      }
+    };
+    auto xu = [&](int q) {
+      const int a = ty + kTbRows * q, k = a * RJ + c;
+      if (a < RI - 1 && c < RJ - 1) {
+        sLX[k] = sLX[k] + (sV2[k] - sV2[k + 1]);
+        sLY[k] = sLY[k] + (sV1[k] - sV1[k + RJ]);
+      }
+    };
+    if (src_h) {
+      tb_sources<true>(t, 1, n0 + nsub, ri0, rj0, RI, RJ, sLE, sLX, sLY);
+      __syncthreads();
+    }
+  #pragma unroll
+    for (int q = 0; q < Q; ++q) hw(q);
+    __syncthreads();
     for (int s = nsub - 1; s >= 0; --s) {
       const int n = n0 + s + 1;
-      if (src_h) {
-        tb_sources<true>(t, 1, n, ri0, rj0, RI, RJ, sLE, sLX, sLY);
-        __syncthreads();
-      }
-      // H half: the curl weight of every Hx / Hy point, then lambda_E gathers
   #pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const int k = (ty + kTbRows * q) * RJ + c;
-        sW1[k] = (fl[q] & kTmzPlainX) ? pt[q].cxn * sLX[k]
-                 : (PSI && (fl[q] & kTmzPsiX))
-                     ? adjx_cpml<P, true>(g, fl[q], pt[q].cxn, j, sLX[k], sP + 2 * NP + k,
-                                          sP + 2 * NP + k)
-                     : 0.f;
-        sW2[k] = (fl[q] & kTmzPlainY) ? pt[q].cy * sLY[k]
-                 : (PSI && (fl[q] & kTmzPsiY))
-                     ? adjy_cpml<P, true>(g, fl[q], pt[q].cy, li[q], sLY[k], sP + 3 * NP + k,
-                                          sP + 3 * NP + k)
-                     : 0.f;
-      }
-      __syncthreads();
-  #pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const int a = ty + kTbRows * q, k = a * RJ + c;
-        if (a >= 1 && c >= 1) {
-          float le = sLE[k];
-          if (fl[q] & kTmzMonitor) {
-            bool has;
-            le = le + P::from_double(seed_of(g, t, b, li[q], j, n, &has));
-          }
-          sLE[k] = le + ((sW1[k - 1] - sW1[k]) + (sW2[k - RJ] - sW2[k]));
-        }
-      }
-      __syncthreads();
+      for (int q = 0; q < Q; ++q) eu(q, n);
       if (src_e) {
+        __syncthreads();
         tb_sources<true>(t, 0, n, ri0, rj0, RI, RJ, sLE, sLX, sLY);
         __syncthreads();
       }
-      // E half: the curl weights of every Ez point (and the gradient on tile
-      // design pixels), then lambda_X / lambda_Y gather them
   #pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const int k = (ty + kTbRows * q) * RJ + c;
-        float w1, w2;
-        if (fl[q] & kTmzPlainE) {
-          const float le = sLE[k];
-          w1 = pt[q].c1 * le;
-          w2 = pt[q].c2n * le;
-        } else {
-          w1 = w2 = 0.f;
-          if (PSI && (fl[q] & kTmzPsiE))
-            adje_cpml<P, true, true, true>(g, fl[q], pt[q].c1, li[q], j, sLE[k], sP + k, sP + k,
-                                           sP + NP + k, sP + NP + k, w1, w2);
-        }
-        sW1[k] = w1;
-        sW2[k] = w2;
-        if ((fl[q] & kTmzDesign) && (fl[q] >> 31)) {
-          const int64_t kk = (int64_t)b * nd + design_index(t, li[q], j);
-          const double le = (double)sLE[k];
-          const double inc = (double)static_cast<const float*>(
-              t.hist)[((int64_t)(n - step0 - 1) * t.nb + b) * nd + (kk - (int64_t)b * nd)];
-          t.grad[kk] += le * inc * t.dc[kk].neg_reps;
-        }
-      }
+      for (int q = 0; q < Q; ++q) ew(q, n);
       __syncthreads();
   #pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const int a = ty + kTbRows * q, k = a * RJ + c;
-        if (a < RI - 1 && c < RJ - 1) {
-          sLX[k] = sLX[k] + (sW2[k] - sW2[k + 1]);
-          sLY[k] = sLY[k] + (sW1[k] - sW1[k + RJ]);
+      for (int q = 0; q < Q; ++q) xu(q);
+      if (s > 0) {
+        if (src_h) {
+          __syncthreads();
+          tb_sources<true>(t, 1, n - 1, ri0, rj0, RI, RJ, sLE, sLX, sLY);
+          __syncthreads();
         }
+  #pragma unroll
+        for (int q = 0; q < Q; ++q) hw(q);
       }
       __syncthreads();
     }
@@ -975,10 +996,13 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
 }
 
 // Region of both blocked kernels: 32 x 64 points; forward 7 arrays (56 KB),
-// adjoint 9 arrays (72 KB) of shared memory.
+// adjoint 11 arrays (88 KB) of shared memory.  (Adjoint measured on GB300,
+// 512^2 x 64 designs, 2000 steps: 9 arrays and four barriers per step
+// 0.3168 s, 11 arrays and two barriers 0.3147 s, and with each design
+// pixel's gradient summed in shared memory over a launch, 104 KB, 0.3266 s.)
 constexpr int kTbFwdRI = kTbRI, kTbAdjRI = kTbRI;
 constexpr size_t kTbFwdSmem = (size_t)7 * kTbFwdRI * kTbRJ * sizeof(float);
-constexpr size_t kTbAdjSmem = (size_t)9 * kTbAdjRI * kTbRJ * sizeof(float);
+constexpr size_t kTbAdjSmem = (size_t)11 * kTbAdjRI * kTbRJ * sizeof(float);
 
 template <int RI>
 dim3 tb_grid(const TmzDev& t) {

@@ -55,17 +55,52 @@ namespace {
 #ifndef GMES_CELL_BLOCKS_DF
 #define GMES_CELL_BLOCKS_DF 10
 #endif
-template <class P>
+// The H half (GMES_CELL_BLOCKS_F64_H / _F32_H / _DF_H) and the E half of
+// dispersive grids (the kernel with the Drude / Lorentz / DCP updates, _D)
+// take their own budgets.  Measured on GB300, ms per half-step:
+//   df64 H, 256^3 cube, 10 / 9 / 8 blocks: 0.3275 / 0.3403 / 0.3223 (8: 64
+//     registers, no spills; at 10 the hot path spilled)
+//   dispersive E, 192^3, blocks 12 or 10 (the E budget) / 9 / 8 / 7 / 6:
+//     FP32 0.1937 / 0.1701 / 0.1812 / -      / -      (9: no spills)
+//     df64 0.2733 / 0.2581 / 0.2693 / 0.2574 / 0.2751
+//     FP64 0.4052 (9) / -   / 0.4041 / 0.4035 / 0.4107
+//   (FP32 H at 10 blocks and FP64 H at 8 ran 1-2 % slower than their E
+//   budgets.)
+#ifndef GMES_CELL_BLOCKS_F64_H
+#define GMES_CELL_BLOCKS_F64_H GMES_CELL_BLOCKS_F64
+#endif
+#ifndef GMES_CELL_BLOCKS_F32_H
+#define GMES_CELL_BLOCKS_F32_H GMES_CELL_BLOCKS_F32
+#endif
+#ifndef GMES_CELL_BLOCKS_DF_H
+#define GMES_CELL_BLOCKS_DF_H 8
+#endif
+#ifndef GMES_CELL_BLOCKS_F64_D
+#define GMES_CELL_BLOCKS_F64_D 7
+#endif
+#ifndef GMES_CELL_BLOCKS_F32_D
+#define GMES_CELL_BLOCKS_F32_D 9
+#endif
+#ifndef GMES_CELL_BLOCKS_DF_D
+#define GMES_CELL_BLOCKS_DF_D 9
+#endif
+constexpr int cell_blocks(int e, int h, int d, int side, bool disp) {
+  return (side == 1 ? h : (disp ? d : e)) * 128 / kCellThreads;
+}
+template <class P, int SIDE, bool DISP>
 struct CellMinBlocks {
-  static constexpr int value = GMES_CELL_BLOCKS_F64 * 128 / kCellThreads;
+  static constexpr int value = cell_blocks(GMES_CELL_BLOCKS_F64, GMES_CELL_BLOCKS_F64_H,
+                                           GMES_CELL_BLOCKS_F64_D, SIDE, DISP);
 };
-template <>
-struct CellMinBlocks<PolF32> {
-  static constexpr int value = GMES_CELL_BLOCKS_F32 * 128 / kCellThreads;
+template <int SIDE, bool DISP>
+struct CellMinBlocks<PolF32, SIDE, DISP> {
+  static constexpr int value = cell_blocks(GMES_CELL_BLOCKS_F32, GMES_CELL_BLOCKS_F32_H,
+                                           GMES_CELL_BLOCKS_F32_D, SIDE, DISP);
 };
-template <>
-struct CellMinBlocks<PolDF> {
-  static constexpr int value = GMES_CELL_BLOCKS_DF * 128 / kCellThreads;
+template <int SIDE, bool DISP>
+struct CellMinBlocks<PolDF, SIDE, DISP> {
+  static constexpr int value = cell_blocks(GMES_CELL_BLOCKS_DF, GMES_CELL_BLOCKS_DF_H,
+                                           GMES_CELL_BLOCKS_DF_D, SIDE, DISP);
 };
 // The multi-grid cell kernels carry a tile loop and a grid look-up on top of
 // the cell body (GMES_MULTI_BLOCKS_F64 / _F32 / _DF override the budgets).
@@ -992,7 +1027,7 @@ __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, i
 }
 
 template <class P, int SIDE, bool STRICT, bool DISP, int MASK, class I>
-__global__ void __launch_bounds__(kCellThreads, CellMinBlocks<P>::value)
+__global__ void __launch_bounds__(kCellThreads, CellMinBlocks<P, SIDE, DISP>::value)
     k_cell(const GridDev g, int bx_log2, int i0) {
   const int bx = 1 << bx_log2;
   const int tx = threadIdx.x & (bx - 1);
