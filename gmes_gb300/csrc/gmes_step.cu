@@ -116,17 +116,42 @@ struct CellMinBlocks<PolDF, SIDE, DISP> {
 #ifndef GMES_MULTI_BLOCKS_DF
 #define GMES_MULTI_BLOCKS_DF 10
 #endif
-template <class P>
+// The H half (_H) and the E half of dispersive grids (_D) may take their
+// own budgets; by default the precision's.  (FP64, 34 grids of the serving
+// mix below 2^20 cells, 25 of them dispersive, ms per 64-step chunk: 141.5
+// at 9 blocks; H at 8 / 7 blocks 143.6 / 146.5, dispersive E at 7 145.1.)
+#ifndef GMES_MULTI_BLOCKS_F64_H
+#define GMES_MULTI_BLOCKS_F64_H GMES_MULTI_BLOCKS_F64
+#endif
+#ifndef GMES_MULTI_BLOCKS_F32_H
+#define GMES_MULTI_BLOCKS_F32_H GMES_MULTI_BLOCKS_F32
+#endif
+#ifndef GMES_MULTI_BLOCKS_DF_H
+#define GMES_MULTI_BLOCKS_DF_H GMES_MULTI_BLOCKS_DF
+#endif
+#ifndef GMES_MULTI_BLOCKS_F64_D
+#define GMES_MULTI_BLOCKS_F64_D GMES_MULTI_BLOCKS_F64
+#endif
+#ifndef GMES_MULTI_BLOCKS_F32_D
+#define GMES_MULTI_BLOCKS_F32_D GMES_MULTI_BLOCKS_F32
+#endif
+#ifndef GMES_MULTI_BLOCKS_DF_D
+#define GMES_MULTI_BLOCKS_DF_D GMES_MULTI_BLOCKS_DF
+#endif
+template <class P, int SIDE, bool DISP>
 struct MultiMinBlocks {
-  static constexpr int value = GMES_MULTI_BLOCKS_F64 * 128 / kBatchThreads;
+  static constexpr int value = cell_blocks(GMES_MULTI_BLOCKS_F64, GMES_MULTI_BLOCKS_F64_H,
+                                           GMES_MULTI_BLOCKS_F64_D, SIDE, DISP);
 };
-template <>
-struct MultiMinBlocks<PolF32> {
-  static constexpr int value = GMES_MULTI_BLOCKS_F32 * 128 / kBatchThreads;
+template <int SIDE, bool DISP>
+struct MultiMinBlocks<PolF32, SIDE, DISP> {
+  static constexpr int value = cell_blocks(GMES_MULTI_BLOCKS_F32, GMES_MULTI_BLOCKS_F32_H,
+                                           GMES_MULTI_BLOCKS_F32_D, SIDE, DISP);
 };
-template <>
-struct MultiMinBlocks<PolDF> {
-  static constexpr int value = GMES_MULTI_BLOCKS_DF * 128 / kBatchThreads;
+template <int SIDE, bool DISP>
+struct MultiMinBlocks<PolDF, SIDE, DISP> {
+  static constexpr int value = cell_blocks(GMES_MULTI_BLOCKS_DF, GMES_MULTI_BLOCKS_DF_H,
+                                           GMES_MULTI_BLOCKS_DF_D, SIDE, DISP);
 };
 // Whether a batch of at most kParamJobs grids takes its descriptors from
 // the argument bank (k_multi_cell_arg) or copies them to shared memory per
@@ -1325,7 +1350,7 @@ static_assert(sizeof(GridDev) % 16 == 0, "GridDev is copied as 16-byte words");
 // the single-grid kernel, whose descriptor is a kernel parameter; from
 // shared memory it runs 1.3x slower (measured on GB300, 160^3 cube).
 template <class P, int SIDE, bool STRICT, bool DISP>
-__global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P>::value)
+__global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P, SIDE, DISP>::value)
     k_multi_cell(const BatchView v, int s) {
   __shared__ __align__(16) unsigned char desc[sizeof(GridDev)];
   const GridDev& g = *reinterpret_cast<const GridDev*>(desc);
@@ -1373,7 +1398,7 @@ __global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P>::value)
 // The same with the descriptors in the kernel's argument bank (batches of
 // at most kParamJobs grids): no shared-memory copy and no barrier per tile.
 template <class P, int SIDE, bool STRICT, bool DISP>
-__global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P>::value)
+__global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P, SIDE, DISP>::value)
     k_multi_cell_arg(const BatchView v, int s, const __grid_constant__ BatchDescs d) {
   const int64_t per = (v.tiles + gridDim.x - 1) / gridDim.x;
   const int64_t b0 = (int64_t)blockIdx.x * per;
