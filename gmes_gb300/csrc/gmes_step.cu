@@ -65,7 +65,10 @@ namespace {
 //     df64 0.2733 / 0.2581 / 0.2693 / 0.2574 / 0.2751
 //     FP64 0.4052 (9) / -   / 0.4041 / 0.4035 / 0.4107
 //   (FP32 H at 10 blocks and FP64 H at 8 ran 1-2 % slower than their E
-//   budgets.)
+//   budgets.  Re-measured with these: 256^3 cube df64 E at 8 blocks 0.329
+//   vs 0.316; FP32 E / H at 9 or 8 blocks 0.230 / 0.254 vs 0.203 / 0.205,
+//   H alone at 9 0.254; FP64 E at 8 0.4485 vs 0.4435, H at 7 0.4638 vs
+//   0.4428.)
 #ifndef GMES_CELL_BLOCKS_F64_H
 #define GMES_CELL_BLOCKS_F64_H GMES_CELL_BLOCKS_F64
 #endif
