@@ -178,8 +178,21 @@ GridDev make_grid_dev(const gmes_grid_desc& g) {
   return d;
 }
 
+// Tile numbering of a grid with blocks of 2^l cells along k.
+TileDiv tile_div(int l, const int32_t n[3]) {
+  TileDiv t;
+  std::memset(&t, 0, sizeof(t));
+  const int64_t bx = int64_t(1) << l, by = kBatchThreads / bx;
+  t.bxl = l;
+  t.nkb = (uint32_t)((n[2] + bx - 1) / bx);
+  t.plane = t.nkb * (uint32_t)((n[1] + by - 1) / by);
+  tile_div_of(t.nkb, t.m_nkb, t.s_nkb);
+  tile_div_of(t.plane, t.m_plane, t.s_plane);
+  return t;
+}
+
 struct BatchLayout {
-  int64_t jobs, tile_prefix, bxl, steps, ghost_prefix, src_prefix, total;
+  int64_t jobs, tile_prefix, td, steps, ghost_prefix, src_prefix, total;
 };
 
 BatchLayout batch_layout(int32_t njobs) {
@@ -189,8 +202,8 @@ BatchLayout batch_layout(int32_t njobs) {
   off = align256(off + (int64_t)njobs * (int64_t)sizeof(GridDev));
   L.tile_prefix = off;
   off = align256(off + (int64_t)(njobs + 1) * 8);
-  L.bxl = off;
-  off = align256(off + (int64_t)njobs * 4);
+  L.td = off;
+  off = align256(off + (int64_t)njobs * (int64_t)sizeof(TileDiv));
   L.steps = off;
   off = align256(off + (int64_t)njobs * 4);
   L.ghost_prefix = off;
@@ -207,7 +220,7 @@ BatchView batch_view(const gmes_batch& b) {
   BatchView v;
   v.jobs = reinterpret_cast<const GridDev*>(w + L.jobs);
   v.tile_prefix = reinterpret_cast<const int64_t*>(w + L.tile_prefix);
-  v.bxl = reinterpret_cast<const int32_t*>(w + L.bxl);
+  v.td = reinterpret_cast<const TileDiv*>(w + L.td);
   v.steps = reinterpret_cast<const int32_t*>(w + L.steps);
   v.ghost_prefix = reinterpret_cast<const int64_t*>(w + L.ghost_prefix);
   v.src_prefix = reinterpret_cast<const int32_t*>(w + L.src_prefix);
@@ -565,7 +578,7 @@ gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs
   std::vector<char> host(L.total, 0);
   GridDev* jobs = reinterpret_cast<GridDev*>(host.data() + L.jobs);
   int64_t* tp = reinterpret_cast<int64_t*>(host.data() + L.tile_prefix);
-  int32_t* bxl = reinterpret_cast<int32_t*>(host.data() + L.bxl);
+  TileDiv* td = reinterpret_cast<TileDiv*>(host.data() + L.td);
   int32_t* steps = reinterpret_cast<int32_t*>(host.data() + L.steps);
   int64_t* gp = reinterpret_cast<int64_t*>(host.data() + L.ghost_prefix);
   int32_t* sp = reinterpret_cast<int32_t*>(host.data() + L.src_prefix);
@@ -593,9 +606,8 @@ gmes_status gmes_batch_prepare(const gmes_grid_desc* const* grids, int32_t njobs
                   q);
     int l = 0;
     while (l < bx_cap && (1 << l) < g->n[2]) ++l;
-    bxl[q] = l;
-    const int64_t bx = 1 << l, by = kBatchThreads / bx;
-    const int64_t tiles = ((g->n[2] + bx - 1) / bx) * ((g->n[1] + by - 1) / by) * g->n[0];
+    td[q] = tile_div(l, g->n);
+    const int64_t tiles = (int64_t)td[q].plane * g->n[0];
     tp[q + 1] = tp[q] + tiles;
     gp[q + 1] = gp[q] + 6 * max_ghost_plane(jobs[q]);
     sp[q + 1] = sp[q] + g->nsrc;
@@ -1088,7 +1100,7 @@ namespace gmes {
 namespace {
 
 constexpr int64_t kNoAllocBytes = 192 * 1024;  // >= batch_layout(GMES_NOALLOC_MAX_GRIDS).total
-static_assert(GMES_NOALLOC_MAX_GRIDS * sizeof(GridDev) + 8192 <= kNoAllocBytes,
+static_assert(GMES_NOALLOC_MAX_GRIDS * (sizeof(GridDev) + sizeof(TileDiv)) + 8192 <= kNoAllocBytes,
               "fixed batch table too small for GMES_NOALLOC_MAX_GRIDS grids");
 
 // The batch tables of gmes_batch_step_noalloc.  Host code never touches this
@@ -1153,7 +1165,7 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
   std::memset(img, 0, (size_t)L.total);
   GridDev* jobs = reinterpret_cast<GridDev*>(img + L.jobs);
   int64_t* tp = reinterpret_cast<int64_t*>(img + L.tile_prefix);
-  int32_t* bxl = reinterpret_cast<int32_t*>(img + L.bxl);
+  TileDiv* td = reinterpret_cast<TileDiv*>(img + L.td);
   int32_t* stp = reinterpret_cast<int32_t*>(img + L.steps);
   int64_t* gp = reinterpret_cast<int64_t*>(img + L.ghost_prefix);
   int32_t* sp = reinterpret_cast<int32_t*>(img + L.src_prefix);
@@ -1182,9 +1194,8 @@ extern "C" gmes_status gmes_batch_step_noalloc(const gmes_grid_desc* const* grid
                   q);
     int l = 0;
     while (l < bx_cap && (1 << l) < g->n[2]) ++l;
-    bxl[q] = l;
-    const int64_t bx = 1 << l, by = kBatchThreads / bx;
-    const int64_t tiles = ((g->n[2] + bx - 1) / bx) * ((g->n[1] + by - 1) / by) * g->n[0];
+    td[q] = tile_div(l, g->n);
+    const int64_t tiles = (int64_t)td[q].plane * g->n[0];
     tp[q + 1] = tp[q] + tiles;
     gp[q + 1] = gp[q] + 6 * max_ghost_plane(jobs[q]);
     sp[q + 1] = sp[q] + g->nsrc;

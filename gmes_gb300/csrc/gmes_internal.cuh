@@ -338,10 +338,40 @@ inline bool offsets_fit_i32(const GridDev& d) {
   return true;
 }
 
+// How a grid's tiles (blocks of the cell kernel) are numbered in the
+// multi-grid kernels: tile t of the grid lies in plane i = t / plane, block
+// row jb = (t - i plane) / nkb and block column kb = t - i plane - jb nkb.
+// Each quotient is a product and a shift (tile_quot) with the multiplier
+// and shift from tile_div_of, exact for t < 2^31.
+struct TileDiv {
+  int32_t bxl;              // log2 of the block's k extent
+  uint32_t nkb;             // blocks per row along k
+  uint32_t plane;           // blocks per plane (nkb x blocks along j)
+  uint32_t m_nkb, m_plane;  // multipliers of / nkb and / plane
+  int32_t s_nkb, s_plane;   // their shifts
+  int32_t pad;
+};
+
+// n / d = (n m) >> s for 0 <= n < 2^31 and 1 <= d < 2^31, with l = ceil(log2
+// d), m = ceil(2^(31+l) / d) (below 2^32) and s = 31 + l: n m / 2^s exceeds
+// n / d by less than n / 2^s < 2^-l <= 1 / d, which never reaches the next
+// integer.
+inline void tile_div_of(uint32_t d, uint32_t& m, int32_t& s) {
+  int l = 0;
+  while ((uint64_t(1) << l) < d) ++l;
+  const uint64_t p = uint64_t(1) << (31 + l);
+  m = (uint32_t)((p + d - 1) / d);
+  s = 31 + l;
+}
+
+__device__ __forceinline__ unsigned tile_quot(unsigned n, unsigned m, int s) {
+  return (unsigned)(((unsigned long long)n * m) >> s);
+}
+
 struct BatchView {
   const GridDev* jobs;
   const int64_t* tile_prefix;   // [njobs + 1] blocks of each grid's half-step
-  const int32_t* bxl;           // per grid: log2 of the block's k extent
+  const TileDiv* td;            // per grid: tile numbering
   const int32_t* steps;         // per grid: steps to take in this chunk
   const int64_t* ghost_prefix;  // [njobs + 1] 6 x (largest ghost plane) per grid
   const int32_t* src_prefix;    // [njobs + 1] point sources

@@ -1376,15 +1376,16 @@ __global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P, SIDE, DISP>::
       __syncthreads();
       cached = job;
     }
-    const int bxl = __ldg(v.bxl + job);
+    const TileDiv& td = v.td[job];
+    const int bxl = __ldg(&td.bxl);
     const int bx = 1 << bxl, by = kBatchThreads >> bxl;
-    const int nkb = (g.n[2] + bx - 1) / bx, njb = (g.n[1] + by - 1) / by;
-    // a grid has fewer than 2^31 tiles: 32-bit unsigned divisions
+    // a grid has fewer than 2^31 tiles: quotients by multiply and shift
     const unsigned local = (unsigned)(b - __ldg(v.tile_prefix + job));
-    const unsigned plane = (unsigned)nkb * (unsigned)njb;
-    const int i = (int)(local / plane);
+    const unsigned plane = __ldg(&td.plane), nkb = __ldg(&td.nkb);
+    const int i = (int)tile_quot(local, __ldg(&td.m_plane), __ldg(&td.s_plane));
     const unsigned rem = local - (unsigned)i * plane;
-    const int jb = (int)(rem / (unsigned)nkb), kb = (int)(rem - (unsigned)jb * nkb);
+    const unsigned jq = tile_quot(rem, __ldg(&td.m_nkb), __ldg(&td.s_nkb));
+    const int jb = (int)jq, kb = (int)(rem - jq * nkb);
     const int k = kb * bx + (threadIdx.x & (bx - 1));
     const int j = jb * by + (threadIdx.x >> bxl);
     // batched grids hold fewer than 2^31 points per component (checked when
@@ -1410,14 +1411,16 @@ __global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P, SIDE, DISP>::
     const int job = find_job<int64_t>(v.tile_prefix, v.njobs, b);  // block-uniform
     if (s >= __ldg(v.steps + job)) continue;
     const GridDev& g = d.jobs[job];
-    const int bxl = __ldg(v.bxl + job);
+    const TileDiv& td = v.td[job];
+    const int bxl = __ldg(&td.bxl);
     const int bx = 1 << bxl, by = kBatchThreads >> bxl;
-    const int nkb = (g.n[2] + bx - 1) / bx, njb = (g.n[1] + by - 1) / by;
+    // a grid has fewer than 2^31 tiles: quotients by multiply and shift
     const unsigned local = (unsigned)(b - __ldg(v.tile_prefix + job));
-    const unsigned plane = (unsigned)nkb * (unsigned)njb;
-    const int i = (int)(local / plane);
+    const unsigned plane = __ldg(&td.plane), nkb = __ldg(&td.nkb);
+    const int i = (int)tile_quot(local, __ldg(&td.m_plane), __ldg(&td.s_plane));
     const unsigned rem = local - (unsigned)i * plane;
-    const int jb = (int)(rem / (unsigned)nkb), kb = (int)(rem - (unsigned)jb * nkb);
+    const unsigned jq = tile_quot(rem, __ldg(&td.m_nkb), __ldg(&td.s_nkb));
+    const int jb = (int)jq, kb = (int)(rem - jq * nkb);
     const int k = kb * bx + (threadIdx.x & (bx - 1));
     const int j = jb * by + (threadIdx.x >> bxl);
     if (k < g.n[2] && j < g.n[1]) {
