@@ -109,7 +109,9 @@ struct CellMinBlocks<PolDF, SIDE, DISP> {
 // the cell body (GMES_MULTI_BLOCKS_F64 / _F32 / _DF override the budgets).
 // Measured on GB300 (one 160^3 cube in a batch, descriptors as launch
 // arguments, ms per step): FP32 at 8 / 10 / 12 blocks 0.203 / 0.174 / 0.187;
-// FP64 at 7 / 8 / 9 blocks 0.304 / 0.302 / 0.292.
+// FP64 at 7 / 8 / 9 blocks 0.304 / 0.302 / 0.292.  Re-measured with chunks
+// replayed as CUDA graphs and the tile range from the host: FP32 at 10 / 12
+// blocks 0.158 / 0.164; df64 at 9 / 10 / 12 blocks 0.224 / 0.236 / 0.246.
 #ifndef GMES_MULTI_BLOCKS_F64
 #define GMES_MULTI_BLOCKS_F64 9
 #endif
@@ -117,7 +119,7 @@ struct CellMinBlocks<PolDF, SIDE, DISP> {
 #define GMES_MULTI_BLOCKS_F32 10
 #endif
 #ifndef GMES_MULTI_BLOCKS_DF
-#define GMES_MULTI_BLOCKS_DF 10
+#define GMES_MULTI_BLOCKS_DF 9
 #endif
 // The H half (_H) and the E half of dispersive grids (_D) may take their
 // own budgets; by default the precision's.  (FP64, 34 grids of the serving
@@ -1354,14 +1356,14 @@ static_assert(sizeof(GridDev) % 16 == 0, "GridDev is copied as 16-byte words");
 // shared memory it runs 1.3x slower (measured on GB300, 160^3 cube).
 template <class P, int SIDE, bool STRICT, bool DISP>
 __global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P, SIDE, DISP>::value)
-    k_multi_cell(const BatchView v, int s) {
+    k_multi_cell(const BatchView v, int s, int64_t per) {
   __shared__ __align__(16) unsigned char desc[sizeof(GridDev)];
   const GridDev& g = *reinterpret_cast<const GridDev*>(desc);
   int cached = -1;
   // a persistent grid (fewer blocks than tiles) gives each block a
-  // contiguous range of tiles, so that a block mostly stays on one grid and
-  // copies its descriptor once
-  const int64_t per = (v.tiles + gridDim.x - 1) / gridDim.x;
+  // contiguous range of per tiles (ceil(tiles / blocks), from the host: a
+  // 64-bit division here cost every thread tens of instructions), so that a
+  // block mostly stays on one grid and copies its descriptor once
   const int64_t b0 = (int64_t)blockIdx.x * per;
   const int64_t b1 = b0 + per < v.tiles ? b0 + per : v.tiles;
   for (int64_t b = b0; b < b1; ++b) {
@@ -1403,8 +1405,7 @@ __global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P, SIDE, DISP>::
 // at most kParamJobs grids): no shared-memory copy and no barrier per tile.
 template <class P, int SIDE, bool STRICT, bool DISP>
 __global__ void __launch_bounds__(kBatchThreads, MultiMinBlocks<P, SIDE, DISP>::value)
-    k_multi_cell_arg(const BatchView v, int s, const __grid_constant__ BatchDescs d) {
-  const int64_t per = (v.tiles + gridDim.x - 1) / gridDim.x;
+    k_multi_cell_arg(const BatchView v, int s, int64_t per, const __grid_constant__ BatchDescs d) {
   const int64_t b0 = (int64_t)blockIdx.x * per;
   const int64_t b1 = b0 + per < v.tiles ? b0 + per : v.tiles;
   for (int64_t b = b0; b < b1; ++b) {
@@ -1543,6 +1544,7 @@ cudaError_t run_batch(const BatchView& v, const GridDev* host_jobs, bool disp, i
                       int blocks, cudaStream_t st) {
   using T = typename P::T;
   const int cells = blocks > 0 ? blocks : (int)(v.tiles < (1 << 30) ? v.tiles : (1 << 30));
+  const int64_t per = cells > 0 ? (v.tiles + cells - 1) / cells : 0;  // tiles per block
   const int gblocks = (int)((v.ghosts + 255) / 256 < 65535 * 16 ? (v.ghosts + 255) / 256 : 65535 * 16);
   const int sblocks = (v.srcs + 127) / 128;
   const bool arg = ArgDescs<P>::value && host_jobs != nullptr && v.njobs <= kParamJobs;
@@ -1558,19 +1560,19 @@ cudaError_t run_batch(const BatchView& v, const GridDev* host_jobs, bool disp, i
         if (arg) {
           if (side == 0) {
             if (disp)
-              k_multi_cell_arg<P, 0, STRICT, true><<<cells, kBatchThreads, 0, st>>>(v, s, descs);
+              k_multi_cell_arg<P, 0, STRICT, true><<<cells, kBatchThreads, 0, st>>>(v, s, per, descs);
             else
-              k_multi_cell_arg<P, 0, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s, descs);
+              k_multi_cell_arg<P, 0, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s, per, descs);
           } else {
-            k_multi_cell_arg<P, 1, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s, descs);
+            k_multi_cell_arg<P, 1, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s, per, descs);
           }
         } else if (side == 0) {
           if (disp)
-            k_multi_cell<P, 0, STRICT, true><<<cells, kBatchThreads, 0, st>>>(v, s);
+            k_multi_cell<P, 0, STRICT, true><<<cells, kBatchThreads, 0, st>>>(v, s, per);
           else
-            k_multi_cell<P, 0, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s);
+            k_multi_cell<P, 0, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s, per);
         } else {
-          k_multi_cell<P, 1, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s);
+          k_multi_cell<P, 1, STRICT, false><<<cells, kBatchThreads, 0, st>>>(v, s, per);
         }
       }
       if (sblocks > 0) k_multi_sources<P, STRICT><<<sblocks, 128, 0, st>>>(v, side, s);
