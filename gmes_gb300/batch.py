@@ -24,8 +24,14 @@ from .scene import source_values
 # Grids of at least this many cells run their own single-grid kernels in a
 # batch.  Measured on GB300 (64-job FP64 serving mix, 2-D 128^2-1024^2 and
 # 3-D 64^3-160^3): the multi-grid kernel alone ran the mix at 8.47 Gcell/s
-# against 8.74 one grid at a time.
-SOLO_CELLS = 1 << 20
+# against 8.74 one grid at a time.  The 34 grids of that mix below 2^20
+# cells (25 dispersive), ms per 64-step chunk with the threshold at 2^20 /
+# 2^19 / 2^18 / 2^17 cells: FP64 138.7 / 122.1 / 119.8 / 121.0, FP32 111.6
+# / 78.4 / 72.8 / 73.6 -- a grid of 2^18 cells (64^3) fills the GPU's
+# resident blocks once over, and the multi-grid kernel runs its cells up to
+# 1.3x slower than the single-grid kernel (and a batch with one dispersive
+# grid runs the dispersive E kernel for all of them).
+SOLO_CELLS = 1 << 18
 
 
 class Batch:

@@ -385,7 +385,8 @@ def saturated_step_seconds(scene, precision="fp64", min_cells=1 << 21, max_copie
     ``copies`` = min(max_copies, ceil(min_cells / cells)) grids of ``scene``
     advance together through ``Batch`` (one multi-grid launch per kernel
     kind and half-step; a grid of SOLO_CELLS cells or more runs its own
-    single-grid kernels, which fill the GPU by themselves); the device time
+    single-grid kernels, which fill the GPU by themselves and run its cells
+    faster than the multi-grid kernel); the device time
     of ``steps`` steps (CUDA events, after a warm-up chunk) divided by
     copies x steps is the grid's step time at a saturated GPU -- the least
     time any batching of it can give.  Returns (seconds, copies).
