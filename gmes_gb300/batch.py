@@ -33,6 +33,9 @@ from .scene import source_values
 # grid runs the dispersive E kernel for all of them).
 SOLO_CELLS = 1 << 18
 
+# Side streams for the solo grids of a batch.
+SOLO_STREAMS = 4
+
 
 class Batch:
     """A fixed set of grids stepped together.
@@ -42,10 +45,13 @@ class Batch:
     block per tile).  Both are launch-shape knobs the autotuner sets.
     ``solo_cells``: grids with at least this many cells run their own
     single-grid kernels (0: every grid through the multi-grid kernel).
+    ``solo_streams``: side streams the solo grids' chunks are spread over,
+    so that one grid's last partial wave of blocks overlaps the next grid's
+    (1: all on the batch's stream, one after another).
     """
 
     def __init__(self, engines, bx_cap=0, blocks=0, use_graphs=True, stream=None,
-                 solo_cells=SOLO_CELLS):
+                 solo_cells=SOLO_CELLS, solo_streams=SOLO_STREAMS):
         torch = _torch()
         if not engines:
             raise ValueError("a batch needs at least one grid")
@@ -64,6 +70,9 @@ class Batch:
         self.solo = [i for i, e in enumerate(self.engines)
                      if solo_cells > 0 and e.scene.cells >= solo_cells]
         self.multi = [i for i in range(len(self.engines)) if i not in self.solo]
+        ns = max(1, min(int(solo_streams), len(self.solo)))
+        self._side = ([torch.cuda.Stream(device=self.device) for _ in range(ns)]
+                      if ns > 1 else [])
         for i in self.solo:
             # the multi-grid kernel's conditions, so that a grid is batchable
             # or not whatever its size
@@ -170,6 +179,12 @@ class Batch:
         self.stage(steps, n0s if n0s is not None else [0.0] * len(steps))
         st = C.c_void_p(self.stream.cuda_stream)
         launched = 0
+        run_solo = [i for i in self.solo if steps[i] > 0]
+        side = self._side if len(run_solo) > 1 else []
+        # the side streams start once the source values are staged, and run
+        # alongside the multi-grid chunk; the batch's stream waits for them
+        for ss in side:
+            ss.wait_stream(self.stream)
         km = max((steps[i] for i in self.multi), default=0)
         if km > 0:
             for q, i in enumerate(self.multi):
@@ -180,18 +195,19 @@ class Batch:
             else:
                 N.check(self.lib.gmes_batch_step(C.byref(self.b), km, self.blocks, st))
             launched += km * self._multi_launches_per_step()
-        for i in self.solo:
+        for n, i in enumerate(run_solo):
             s = steps[i]
-            if s <= 0:
-                continue
             e = self.engines[i]
+            sst = C.c_void_p(side[n % len(side)].cuda_stream) if side else st
             # the chunk length every grid shares is replayed as the grid's
             # own graph; a shorter last chunk runs as plain launches
             if self.use_graphs and s == k:
-                N.check(self.lib.gmes_graph_launch(C.c_void_p(e._graph(s)), st))
+                N.check(self.lib.gmes_graph_launch(C.c_void_p(e._graph(s)), sst))
             else:
-                N.check(self.lib.gmes_step(C.byref(e.desc), s, st))
+                N.check(self.lib.gmes_step(C.byref(e.desc), s, sst))
             launched += s * self._solo_launches_per_step(i)
+        for ss in side:
+            self.stream.wait_stream(ss)
         return launched
 
     def synchronize(self):

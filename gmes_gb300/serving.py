@@ -29,7 +29,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .batch import Batch
+from .batch import SOLO_STREAMS, Batch
 from .engine import GridEngine, _torch
 
 
@@ -379,10 +379,13 @@ def run_one_at_a_time(jobs, precision="fp64", device=None, realtime=False):
 
 
 def saturated_step_seconds(scene, precision="fp64", min_cells=1 << 21, max_copies=128,
-                           steps=24, device=None):
+                           steps=24, device=None, min_copies=SOLO_STREAMS):
     """Seconds per step of one grid when copies of it fill the GPU.
 
-    ``copies`` = min(max_copies, ceil(min_cells / cells)) grids of ``scene``
+    ``copies`` = max(min_copies, min(max_copies, ceil(min_cells / cells)))
+    grids of ``scene`` (at least one per side stream of the batch, so that a
+    large grid's last partial wave of blocks overlaps another copy's, as it
+    overlaps other grids in a mix)
     advance together through ``Batch`` (one multi-grid launch per kernel
     kind and half-step; a grid of SOLO_CELLS cells or more runs its own
     single-grid kernels, which fill the GPU by themselves and run its cells
@@ -393,7 +396,7 @@ def saturated_step_seconds(scene, precision="fp64", min_cells=1 << 21, max_copie
     """
     torch = _torch()
     cells = scene.cells
-    copies = int(max(1, min(max_copies, -(-min_cells // max(cells, 1)))))
+    copies = int(max(min_copies, 1, min(max_copies, -(-min_cells // max(cells, 1)))))
     engines = [GridEngine(scene, precision=precision, device=device, src_chunk=steps)
                for _ in range(copies)]
     batch = Batch(engines)

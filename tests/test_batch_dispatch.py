@@ -1,8 +1,9 @@
 """How a Batch chunk is dispatched, on the host: the small grids' step
 counts go to the multi-grid kernel in their order, each large (solo) grid
 replays its own chunk graph when it runs the full chunk and plain launches
-otherwise, and the launch count adds up.  No GPU: the library is a
-recorder."""
+otherwise, solo grids spread over the side streams, which start after the
+staging and join the batch's stream at the end, and the launch count adds
+up.  No GPU: the library and the streams are recorders."""
 import ctypes as C
 import types
 
@@ -17,6 +18,7 @@ from gmes_gb300.batch import Batch  # noqa: E402
 class _Lib:
     def __init__(self):
         self.calls = []
+        self.streams = []  # stream of each solo launch
 
     def gmes_batch_set_steps(self, b, steps, stream):
         self.calls.append(("set_steps", list(steps)))
@@ -24,6 +26,7 @@ class _Lib:
 
     def gmes_graph_launch(self, h, stream):
         self.calls.append(("graph", h.value))
+        self.streams.append(stream.value)
         return 0
 
     def gmes_batch_step(self, b, k, blocks, stream):
@@ -32,6 +35,7 @@ class _Lib:
 
     def gmes_step(self, desc, k, stream):
         self.calls.append(("step", k))
+        self.streams.append(stream.value)
         return 0
 
 
@@ -42,12 +46,21 @@ def _engine(cells, nsrc, handle):
                                  _graph=lambda k, h=handle: h + k)
 
 
+class _Stream:
+    def __init__(self, handle, batch):
+        self.cuda_stream, self.batch = handle, batch
+
+    def wait_stream(self, other):
+        self.batch.lib.calls.append(("wait", self.cuda_stream, other.cuda_stream))
+
+
 def _batch(engines, solo, use_graphs=True):
     b = object.__new__(Batch)
     b.engines, b.solo = engines, solo
     b.multi = [i for i in range(len(engines)) if i not in solo]
     b.lib, b.use_graphs, b.blocks = _Lib(), use_graphs, 0
-    b.stream = types.SimpleNamespace(cuda_stream=7)
+    b.stream = _Stream(7, b)
+    b._side = []
     b.b = N.BatchC()
     b.b.ghosts, b.b.srcs = 10, 1
     b._steps = (C.c_int32 * len(b.multi))()
@@ -82,3 +95,22 @@ def test_all_solo_and_idle_chunks():
     assert b.run([0, 0]) == 0 and b.lib.calls == []
     assert b.run([7, 0]) == 7 * 4
     assert b.lib.calls == [("graph", 1007)]
+
+
+def test_solo_grids_on_side_streams():
+    engines = [_engine(2 << 20, 0, 1000), _engine(2 << 20, 0, 2000), _engine(2 << 20, 0, 3000),
+               _engine(4000, 1, 0)]
+    b = _batch(engines, solo=[0, 1, 2])
+    b._side = [_Stream(8, b), _Stream(9, b)]
+    b.run([16, 16, 16, 16])
+    calls = b.lib.calls
+    # the side streams wait for the staging before the multi-grid chunk is enqueued
+    assert calls[:3] == [("wait", 8, 7), ("wait", 9, 7), ("set_steps", [16])]
+    assert calls[3] == ("graph", 5016)
+    assert calls[4:7] == [("graph", 1016), ("graph", 2016), ("graph", 3016)]
+    assert b.lib.streams == [7, 8, 9, 8]  # the multi-grid chunk, then the solo grids
+    assert calls[7:] == [("wait", 7, 8), ("wait", 7, 9)]
+    # one solo grid left: it runs on the batch's stream, no side streams
+    b.lib = _Lib()
+    b.run([0, 5, 0, 0])
+    assert b.lib.calls == [("graph", 2005)] and b.lib.streams == [7]
