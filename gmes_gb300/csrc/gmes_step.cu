@@ -305,6 +305,7 @@ __device__ __forceinline__ R plain_upd(R F, R c1, R c2, R p1, R p2) {
 // it is inlined.
 __device__ __forceinline__ double madd(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float madd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ df madd(df a, df b, df c) { return df_fma(a, b, c); }
 
 // Update of a CPML point in the separate form (src/pw_cpml.hh:115-132 E,
 // 327-344 H): psi1 = b1 psi1 + (c1/d1) D1 and psi2 likewise where the point
@@ -441,7 +442,8 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
     } else {
       // the float-float type keeps this block inline: in cpml_separate it
       // spilled more and ran 1.5 % slower (256^3 cube, 24.21 -> 23.84
-      // Gcell/s); the arithmetic is the same, term for term
+      // Gcell/s); the arithmetic is cpml_separate's, term for term (its
+      // warp-uniform CPML path takes cpml_separate)
       const Coef* q1 = g.prof[__ldg(&cc.pml)][C][a1] + (int64_t)x[a1] * kProfStride;
       const Coef* q2 = g.prof[__ldg(&cc.pml)][C][a2] + (int64_t)x[a2] * kProfStride;
       const bool on1 = coef_nonzero(q1 + 1), on2 = coef_nonzero(q2 + 1);
@@ -451,16 +453,16 @@ __device__ __forceinline__ void update_fast(const GridDev& g, int64_t lin, const
       }
       R psi1 = pre.a, psi2 = pre.b;
       if (on1) {
-        psi1 = P::cfg(q1) * psi1 + P::cfg(q1 + 3) * p1;
+        psi1 = madd(P::cfg(q1 + 3), p1, P::cfg(q1) * psi1);
         P::st(aux + lin, psi1);
       }
       if (on2) {
-        psi2 = P::cfg(q2) * psi2 + P::cfg(q2 + 3) * p2;
+        psi2 = madd(P::cfg(q2 + 3), p2, P::cfg(q2) * psi2);
         P::st(aux + np + lin, psi2);
       }
-      const R X = ((psi1 - psi2) + P::cfg(q1 + 4) * p1) - P::cfg(q2 + 4) * p2;
+      const R X = madd(-P::cfg(q2 + 4), p2, madd(P::cfg(q1 + 4), p1, psi1 - psi2));
       const R cdt = P::cfg(&cc.cdt);
-      P::st(fp, E ? F + cdt * X : F - cdt * X);
+      P::st(fp, E ? madd(cdt, X, F) : madd(-cdt, X, F));
     }
     return;
   }
@@ -866,11 +868,14 @@ __device__ __forceinline__ void cell_body(const GridDev& g, int i, int j, int k)
 // the per-point kind dispatch.  Measured on GB300 (256^3 cube, Gcell/s, one
 // box): FP32 39.78 -> 40.64; with it df64 ran 24.21 -> 23.01 and FP64 18.90
 // -> 18.91, so only FP32 takes it (GMES_UNIFORM_CPML = 1 gives it every
-// precision, 0 none).  The CPML update it shares with the per-point path
+// precision, 0 none).  Re-measured per half with the per-half register
+// budgets (ms): df64 E 0.3185 -> 0.403, H 0.3245 -> 0.3200; FP64 E 0.4435
+// -> 0.4697, H 0.4428 -> 0.4497; so the float-float type takes it on its H
+// half too.  The CPML update it shares with the per-point path
 // (cpml_separate) fuses every multiply-add explicitly: inlined in two places
 // with implicit contraction, the two copies rounded differently and a grid
 // batched with another warp layout lost bit-identity with its solo run.
-template <class P>
+template <class P, int SIDE>
 struct UniformCpml {
 #if defined(GMES_UNIFORM_CPML)
   static constexpr bool value = GMES_UNIFORM_CPML != 0;
@@ -878,12 +883,20 @@ struct UniformCpml {
   static constexpr bool value = false;
 #endif
 };
-template <>
-struct UniformCpml<PolF32> {
+template <int SIDE>
+struct UniformCpml<PolF32, SIDE> {
 #if defined(GMES_UNIFORM_CPML)
   static constexpr bool value = GMES_UNIFORM_CPML != 0;
 #else
   static constexpr bool value = true;
+#endif
+};
+template <int SIDE>
+struct UniformCpml<PolDF, SIDE> {
+#if defined(GMES_UNIFORM_CPML)
+  static constexpr bool value = GMES_UNIFORM_CPML != 0;
+#else
+  static constexpr bool value = SIDE == 1;
 #endif
 };
 
@@ -971,7 +984,7 @@ __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, i
   // count as dielectric: they are skipped)
   int ka = GMES_KIND_DIELECTRIC, kb = GMES_KIND_DIELECTRIC, kc = GMES_KIND_DIELECTRIC;
   bool fast;
-  if constexpr (UniformCpml<P>::value) {
+  if constexpr (UniformCpml<P, SIDE>::value) {
     if (uniform) {
       if (is_active<MASK, c0>(g)) ka = g.tab[c0][id0].kind;
       if (is_active<MASK, c0 + 1>(g)) kb = g.tab[c0 + 1][id1].kind;
@@ -1001,7 +1014,7 @@ __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, i
             plain_upd<E>(f2, P::cfg(&qc.c1), P::cfg(&qc.c2), d21, d22));
     return;
   }
-  if constexpr (UniformCpml<P>::value) {
+  if constexpr (UniformCpml<P, SIDE>::value) {
     const auto dc = [](int kd) {
       return kd == GMES_KIND_DIELECTRIC || kd == GMES_KIND_CPML;
     };

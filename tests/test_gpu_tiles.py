@@ -37,7 +37,8 @@ SCENES = {
     "bloch48": lambda p: _bloch48(p),
 }
 CASES_RUN = [("cube45", "fp64"), ("cube45", "fp32"), ("cube45", "df64"),
-             ("cube45_kappa4", "fp64"), ("disp40", "fp64"), ("disp40", "fp32"),
+             ("cube45_kappa4", "fp64"), ("cube45_kappa4", "fp32"), ("cube45_kappa4", "df64"),
+             ("disp40", "fp64"), ("disp40", "fp32"),
              ("disp40", "df64"), ("drude2d", "fp64"), ("air2d", "fp64"), ("air2d", "fp32"),
              ("bloch48", "fp64")]
 
