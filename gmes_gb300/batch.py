@@ -4,9 +4,11 @@ A ``Batch`` holds a set of ``GridEngine`` objects of one precision.  Each
 chunk of steps runs as ONE launch per kernel kind per half-step for the
 small grids of the batch (``gmes_batch_step``), captured as a CUDA graph
 per chunk length; grids of ``solo_cells`` cells or more fill the GPU on
-their own and run their single-grid kernels (their own chunk graph) on the
-batch's stream, where the multi-grid kernel's per-block job look-up and
-descriptor loads would only slow them.  Each grid takes its own number of
+their own and run their single-grid kernels (their own chunk graph),
+where the multi-grid kernel's per-block job look-up and descriptor loads
+would only slow them, spread over a few side streams so that one grid's
+last partial wave of blocks overlaps the next grid's and the multi-grid
+chunk.  Each grid takes its own number of
 steps in a chunk, so grids of different sizes and step counts share the
 device without waiting for one another; a grid's arithmetic is the same as
 when it runs alone.
@@ -167,7 +169,9 @@ class Batch:
         """Advance grid i by steps[i] steps (one chunk; max(steps) <= every src_chunk).
 
         ``n0s[i]`` is grid i's current time step (for its source values).
-        Work is enqueued on ``self.stream``; call ``synchronize()`` to wait.
+        Work is enqueued on ``self.stream`` (the solo grids' on side streams
+        that start after the staging and that ``self.stream`` waits for);
+        call ``synchronize()`` to wait.
         Returns the number of kernels it launched.
         """
         steps = [int(s) for s in steps]
