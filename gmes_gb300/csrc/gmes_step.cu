@@ -928,6 +928,21 @@ __device__ __forceinline__ Pre<P> psi_pair(const GridDev& g, int c, int64_t lin)
 // 42.54 -> 30.1 / 29.7 / 34.3 / 31.1 Gcell/s at 6 / 7 / 8 / 10 blocks per SM
 // (64 registers at 8), dispersive FP32 25.42 -> 22.35; df64 (5, 6 blocks)
 // 26.74 -> 17.5 / 20.7, FP64 (6 blocks) 19.25 -> 16.99.
+// Whether a warp on the warp-uniform CPML path reads its classes'
+// plain-form coefficients together with their kinds (one round trip to the
+// class table instead of two).  Measured on GB300 (256^3 cube, ms per E / H
+// half): df64 0.3143 / 0.3192 -> 0.3145 / 0.3135; FP32 0.2044 / 0.2070 ->
+// 0.2269 / 0.2098 (three more live values at 40 registers), so the
+// float-float type only (GMES_EARLY_COEF = 0 / 1 sets it for both).
+template <class P>
+struct EarlyCoef {
+#if defined(GMES_EARLY_COEF)
+  static constexpr bool value = GMES_EARLY_COEF != 0;
+#else
+  static constexpr bool value = std::is_same<P, PolDF>::value;
+#endif
+};
+
 template <class P, int SIDE, bool DISP, int MASK, class I>
 __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, int k) {
   using R = typename P::R;
@@ -984,11 +999,27 @@ __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, i
   // count as dielectric: they are skipped)
   int ka = GMES_KIND_DIELECTRIC, kb = GMES_KIND_DIELECTRIC, kc = GMES_KIND_DIELECTRIC;
   bool fast;
+  // plain-form coefficients of the warp's three classes, read with the kinds
+  // (one round trip to the class table instead of two)
+  R ca1 = P::zero(), ca2 = P::zero(), cb1 = P::zero(), cb2 = P::zero(), cc1 = P::zero(),
+    cc2 = P::zero();
   if constexpr (UniformCpml<P, SIDE>::value) {
     if (uniform) {
-      if (is_active<MASK, c0>(g)) ka = g.tab[c0][id0].kind;
-      if (is_active<MASK, c0 + 1>(g)) kb = g.tab[c0 + 1][id1].kind;
-      if (is_active<MASK, c0 + 2>(g)) kc = g.tab[c0 + 2][id2].kind;
+      if (is_active<MASK, c0>(g)) {
+        const ClassCoef& q = g.tab[c0][id0];
+        ka = q.kind;
+        if (EarlyCoef<P>::value) ca1 = P::cfg(&q.c1), ca2 = P::cfg(&q.c2);
+      }
+      if (is_active<MASK, c0 + 1>(g)) {
+        const ClassCoef& q = g.tab[c0 + 1][id1];
+        kb = q.kind;
+        if (EarlyCoef<P>::value) cb1 = P::cfg(&q.c1), cb2 = P::cfg(&q.c2);
+      }
+      if (is_active<MASK, c0 + 2>(g)) {
+        const ClassCoef& q = g.tab[c0 + 2][id2];
+        kc = q.kind;
+        if (EarlyCoef<P>::value) cc1 = P::cfg(&q.c1), cc2 = P::cfg(&q.c2);
+      }
     }
     fast = uniform && ka == GMES_KIND_DIELECTRIC && kb == GMES_KIND_DIELECTRIC &&
            kc == GMES_KIND_DIELECTRIC;
@@ -1003,6 +1034,15 @@ __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, i
     const ClassCoef& qa = g.tab[c0][id0];
     const ClassCoef& qb = g.tab[c0 + 1][id1];
     const ClassCoef& qc = g.tab[c0 + 2][id2];
+    if (UniformCpml<P, SIDE>::value && EarlyCoef<P>::value) {
+      if (is_active<MASK, c0>(g))
+        P::st(static_cast<T*>(g.f[c0]) + l0, plain_upd<E>(f0, ca1, ca2, d01, d02));
+      if (is_active<MASK, c0 + 1>(g))
+        P::st(static_cast<T*>(g.f[c0 + 1]) + l1, plain_upd<E>(f1, cb1, cb2, d11, d12));
+      if (is_active<MASK, c0 + 2>(g))
+        P::st(static_cast<T*>(g.f[c0 + 2]) + l2, plain_upd<E>(f2, cc1, cc2, d21, d22));
+      return;
+    }
     if (is_active<MASK, c0>(g))
       P::st(static_cast<T*>(g.f[c0]) + l0,
             plain_upd<E>(f0, P::cfg(&qa.c1), P::cfg(&qa.c2), d01, d02));
