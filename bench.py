@@ -607,7 +607,7 @@ def serving_compare(njobs, rate, max_steps, size_scale, precision, bound=True, t
             "saturated_s": round(b["saturated_s"], 3),
             "definition": "sum of the jobs' one-at-a-time wall times over the sum of their "
                           "steps x saturated step time (copies of the grid filling the GPU "
-                          "through the batch: the multi-grid kernel below 2^18 cells, each "
+                          "through the batch: the multi-grid kernel below 2^17 cells, each "
                           "copy's own kernels above; CUDA events)"}
         out["speedup_over_bound"] = round(out["speedup"] / b["bound"], 3)
     return out

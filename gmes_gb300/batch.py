@@ -32,8 +32,12 @@ from .scene import source_values
 # / 78.4 / 72.8 / 73.6 -- a grid of 2^18 cells (64^3) fills the GPU's
 # resident blocks once over, and the multi-grid kernel runs its cells up to
 # 1.3x slower than the single-grid kernel (and a batch with one dispersive
-# grid runs the dispersive E kernel for all of them).
-SOLO_CELLS = 1 << 18
+# grid runs the dispersive E kernel for all of them).  With the solo grids
+# on 4 side streams (below), ms per chunk at 2^18 / 2^17 / 2^16 / 2^14
+# cells: FP64 101.3 / 99.8 / 99.9 / 99.9, FP32 61.1 / 59.3 / 59.3 / 59.2;
+# the multi-grid kernel stays for grids below 2^17 cells (2-D up to ~360^2,
+# 3-D up to ~50^3), where one launch serves many grids.
+SOLO_CELLS = 1 << 17
 
 # Side streams for the solo grids of a batch.
 SOLO_STREAMS = 4
