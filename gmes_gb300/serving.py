@@ -378,6 +378,13 @@ def run_one_at_a_time(jobs, precision="fp64", device=None, realtime=False):
             "job_s": job_s}
 
 
+def saturation_copies(cells, min_cells=1 << 21, max_copies=128, min_copies=SOLO_STREAMS):
+    """Copies of a grid of ``cells`` cells that ``saturated_step_seconds``
+    steps together: enough for ``min_cells`` cells, at most ``max_copies``,
+    and at least ``min_copies`` (one per side stream of the batch)."""
+    return int(max(min_copies, 1, min(max_copies, -(-min_cells // max(int(cells), 1)))))
+
+
 def saturated_step_seconds(scene, precision="fp64", min_cells=1 << 21, max_copies=128,
                            steps=24, device=None, min_copies=SOLO_STREAMS):
     """Seconds per step of one grid when copies of it fill the GPU.
@@ -396,7 +403,7 @@ def saturated_step_seconds(scene, precision="fp64", min_cells=1 << 21, max_copie
     """
     torch = _torch()
     cells = scene.cells
-    copies = int(max(min_copies, 1, min(max_copies, -(-min_cells // max(cells, 1)))))
+    copies = saturation_copies(cells, min_cells, max_copies, min_copies)
     engines = [GridEngine(scene, precision=precision, device=device, src_chunk=steps)
                for _ in range(copies)]
     batch = Batch(engines)

@@ -100,3 +100,15 @@ def test_failed_resident_job_frees_its_share(monkeypatch):
     srv._fail(b, 1.5, "non-finite field values")
     assert srv.used_bytes == 100 and srv.resident_cells == 100
     assert srv.failed == [b] and b.t_finish == 1.5 and b.engine is None
+
+
+def test_saturation_copies():
+    """Copies the batching bound steps together per grid: enough for 2^21
+    cells, at most 128, at least one per side stream of the batch."""
+    from gmes_gb300.batch import SOLO_STREAMS
+    assert S.saturation_copies(1 << 14) == 128              # capped
+    assert S.saturation_copies(1 << 16) == 32               # 2^21 / 2^16
+    assert S.saturation_copies(100_000) == 21               # rounded up
+    assert S.saturation_copies(1 << 20) == max(2, SOLO_STREAMS)
+    assert S.saturation_copies(4096 ** 2) == SOLO_STREAMS   # large grid: one per side stream
+    assert S.saturation_copies(4096 ** 2, min_copies=1) == 1
