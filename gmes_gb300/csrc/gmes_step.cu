@@ -907,27 +907,6 @@ __device__ __forceinline__ Pre<P> psi_pair(const GridDev& g, int c, int64_t lin)
   return {P::ldw(aux + lin), P::ldw(aux + g.npts[c] + lin)};
 }
 
-// The half-step update of one cell in the fast precisions.  Every field
-// value and class id the cell reads is loaded first, so that no load waits
-// for another.  Then a warp whose cells all carry the same class triple, each
-// class of kind DIELECTRIC (one vote, __match_all_sync, and three
-// warp-uniform kind look-ups), updates its three points with those classes'
-// coefficients and nothing else; every other warp goes through the
-// per-point path (update_fast), whose dielectric branch is the same
-// arithmetic, so the two paths agree bit for bit.  The offsets come from
-// the three array-shape families (fst): an active component's strides are
-// its family's.  Measured on GB300 (256^3 cube / 192^3 dispersive scene,
-// Gcell/s, per-point path only -> with the warp-uniform path):
-//   cube FP64 17.42 -> 18.60, FP32 34.17 -> 34.91, df64 21.89 -> 23.63;
-//   dispersive FP64 9.85 -> 10.09, FP32 20.48 -> 22.36, df64 14.85 -> 15.04.
-// A per-warp table of plain warps built at set-up (read with the field
-// values, class maps read only by the other warps) ran slower: cube FP64
-// 18.20, FP32 31.90, df64 22.95.  So did two cells per thread, (i, j, k) and
-// (i + 1, j, k), with the loads of both issued before either update (twice
-// the bytes in flight per warp, four shared neighbour loads): cube FP32
-// 42.54 -> 30.1 / 29.7 / 34.3 / 31.1 Gcell/s at 6 / 7 / 8 / 10 blocks per SM
-// (64 registers at 8), dispersive FP32 25.42 -> 22.35; df64 (5, 6 blocks)
-// 26.74 -> 17.5 / 20.7, FP64 (6 blocks) 19.25 -> 16.99.
 // Whether a warp on the warp-uniform CPML path reads its classes'
 // plain-form coefficients together with their kinds (one round trip to the
 // class table instead of two).  Measured on GB300 (256^3 cube, ms per E / H
@@ -943,6 +922,29 @@ struct EarlyCoef {
 #endif
 };
 
+// The half-step update of one cell in the fast precisions.  Every field
+// value and class id the cell reads is loaded first, so that no load waits
+// for another.  Then a warp whose cells all carry the same class triple, each
+// class of kind DIELECTRIC (one vote, __match_all_sync, and three
+// warp-uniform kind look-ups), updates its three points with those classes'
+// coefficients and nothing else (FP32 and the float-float H half also take
+// warps of one DIELECTRIC or CPML class per component directly:
+// UniformCpml); every other warp goes through the per-point path
+// (update_fast), whose dielectric and CPML branches are the same
+// arithmetic, so the paths agree bit for bit.  The offsets come from
+// the three array-shape families (fst): an active component's strides are
+// its family's.  Measured on GB300 (256^3 cube / 192^3 dispersive scene,
+// Gcell/s, per-point path only -> with the warp-uniform path):
+//   cube FP64 17.42 -> 18.60, FP32 34.17 -> 34.91, df64 21.89 -> 23.63;
+//   dispersive FP64 9.85 -> 10.09, FP32 20.48 -> 22.36, df64 14.85 -> 15.04.
+// A per-warp table of plain warps built at set-up (read with the field
+// values, class maps read only by the other warps) ran slower: cube FP64
+// 18.20, FP32 31.90, df64 22.95.  So did two cells per thread, (i, j, k) and
+// (i + 1, j, k), with the loads of both issued before either update (twice
+// the bytes in flight per warp, four shared neighbour loads): cube FP32
+// 42.54 -> 30.1 / 29.7 / 34.3 / 31.1 Gcell/s at 6 / 7 / 8 / 10 blocks per SM
+// (64 registers at 8), dispersive FP32 25.42 -> 22.35; df64 (5, 6 blocks)
+// 26.74 -> 17.5 / 20.7, FP64 (6 blocks) 19.25 -> 16.99.
 template <class P, int SIDE, bool DISP, int MASK, class I>
 __device__ __forceinline__ void cell_body_fast(const GridDev& g, int i, int j, int k) {
   using R = typename P::R;
