@@ -999,7 +999,11 @@ __global__ void __launch_bounds__(kTbThreads, kTbMinBlocks)
 // adjoint 11 arrays (88 KB) of shared memory.  (Adjoint measured on GB300,
 // 512^2 x 64 designs, 2000 steps: 9 arrays and four barriers per step
 // 0.3168 s, 11 arrays and two barriers 0.3147 s, and with each design
-// pixel's gradient summed in shared memory over a launch, 104 KB, 0.3266 s.)
+// pixel's gradient summed in shared memory over a launch, 104 KB, 0.3266 s;
+// a thread's own curl weights kept in registers from the pass that forms
+// them to the pass that gathers them, four fewer shared-memory loads per
+// point and step but spilling at 64 registers: 0.352 s, the E half's alone
+// 0.328 s, against 0.316 s.)
 constexpr int kTbFwdRI = kTbRI, kTbAdjRI = kTbRI;
 constexpr size_t kTbFwdSmem = (size_t)7 * kTbFwdRI * kTbRJ * sizeof(float);
 constexpr size_t kTbAdjSmem = (size_t)11 * kTbAdjRI * kTbRJ * sizeof(float);
