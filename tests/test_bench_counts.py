@@ -1,6 +1,7 @@
 """Host-side figures of the bench line that need no GPU: the kernel-launch
 count claimed for the differentiation workload, which follows the
-library's chunking of the temporally blocked kernels."""
+library's chunking of the temporally blocked kernels, and the algorithmic
+bytes per half-step behind the roofline fraction."""
 import types
 
 import pytest
@@ -41,3 +42,32 @@ def test_adjoint_chunks_of_the_default_workload():
     # 2000 steps: 500 launches of 4; a 45-step segment: 13 launches (odd)
     assert _adj_chunks(2000, 4) == 500
     assert _adj_chunks(45, 4) == 13 and _adj_chunks(2, 4) == 2 and _adj_chunks(1, 4) == 1
+
+
+@pytest.mark.parametrize("precision,es", [("fp64", 8), ("fp32", 4), ("df64", 8)])
+def test_half_bytes_of_a_cube(precision, es):
+    """E half: every E value read and written, every H value read, one class
+    id per E point, and psi1 / psi2 read and written at every CPML point;
+    the H half likewise with the roles swapped."""
+    import bench
+    from gmes_gb300 import workloads as W
+    sim, _ = W.cube(n=12, nobj=2, pml_cells=3, precision="fp64")
+    scene = sim.compile()
+    e_b, h_b = bench.half_bytes(scene, precision)
+    for side, got in ((0, e_b), (1, h_b)):
+        own = [c for c in range(6) if (c < 3) == (side == 0)]
+        other = [c for c in range(6) if c not in own]
+        want = 0
+        for c in own:
+            n = 1
+            for v in scene.shape(c):
+                n *= v
+            cpml = sum(cnt for cid, cnt in scene.counts(c).items()
+                       if scene.classes[c][cid].kind == 2)  # GMES_KIND_CPML
+            want += 2 * es * n + n + 2 * 2 * es * cpml
+        for c in other:
+            n = 1
+            for v in scene.shape(c):
+                n *= v
+            want += es * n
+        assert got == want, (side, got, want)
